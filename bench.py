@@ -1,0 +1,345 @@
+"""Benchmark of the single-rank ogs GatherScatter on GB300.
+
+Default workload: the reference's headline call, ogs_t::GatherScatter(o_q, 1,
+ogs::Add, ogs::Sym) on an Unsigned handle (dawgsMain.cpp:211-219), fp64, k=1,
+over a 24x24x24-hex box mesh of degree p=7 (7,077,888 local / 4,826,809 global
+nodes), values U[-1,1] from a fixed seed.  The metric is the reference's
+DOFS/s = NgatherGlobal / seconds per call (dawgsMain.cpp:207).
+
+One step = one GatherScatter launch over the whole mesh, inputs resident in
+HBM.  Between steps the field is restored from a pristine device copy and L2
+is flushed by writing a buffer of twice the L2 size (the maps and field, about
+0.1 GB, would otherwise stay in the 126 MB L2); only the GatherScatter is
+inside the CUDA-event timing.  `e2e` is the same metric through the C ABI's
+host-buffer entry point (ogs_gather_scatter_host: pinned host field copied in,
+GatherScatter, copied back, stream synchronised) timed on the host clock.
+`--impl reference` times the CPU oracle -- the C restatement of the
+reference's host ogs (libs/ogs/ogsOperator.cpp:311-360) with its OpenMP row
+loop -- on all host cores, on the same workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "ogs_tiles_kernel_gs_fp64_add_24x24x24_p7.md")
+FALLBACK_HBM_GBS = 6800.0
+TYPE_CODE = {"float32": 0, "float64": 1, "int32": 2, "int64": 3}
+OP_CODE = {"add": 0, "mul": 1, "max": 2, "min": 3}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nx", type=int, default=24)
+    ap.add_argument("--ny", type=int, default=24)
+    ap.add_argument("--nz", type=int, default=24)
+    ap.add_argument("--p", type=int, default=7)
+    ap.add_argument("--dtype", choices=list(TYPE_CODE), default="float64")
+    ap.add_argument("--op", choices=list(OP_CODE), default="add")
+    ap.add_argument("--k", type=int, default=1)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    a = ap.parse_args()
+    a.warmup = max(a.warmup, 3)
+    return a
+
+
+# ------------------------------------------------------------------ helpers
+class Clocks:
+    """nvidia-smi sampler running during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                     timeout=5).stdout.strip()
+                if out:
+                    self.rows.append([x.strip() for x in out.split(",")])
+            except Exception:
+                return
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.rows:
+            return None
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in self.rows for n, val in zip(names, r[5:9]) if val.strip() == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def hbm_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profiled_traffic():
+    """dram bytes per launch from the committed ncu summary (same workload)."""
+    try:
+        for line in open(PROFILE_TRAFFIC):
+            if line.strip().startswith("dram_bytes_per_launch:"):
+                return int(line.split(":")[1].strip().replace(",", ""))
+    except OSError:
+        pass
+    return None
+
+
+def workload_name(a):
+    return f"ogs GatherScatter {a.dtype} {a.op.capitalize()} Sym k={a.k}, {a.nx}x{a.ny}x{a.nz} hex box p={a.p}"
+
+
+def alg_bytes(N, nnz, R, k, s):
+    """GatherScatter (Sym): read and write every local value, read colIds and rowStarts."""
+    return 2 * k * s * N + 4 * nnz + 4 * (R + 1)
+
+
+def make_inputs(a):
+    from dawgs_gb300 import mesh
+    ids = mesh.box_ids(a.nx, a.ny, a.nz, a.p)
+    dt = np.dtype(a.dtype)
+    n = a.k * ids.size
+    if dt.kind == "f":
+        v = mesh.uniform_values(n, dt, 0.5, 2.0, a.seed) if a.op == "mul" else \
+            mesh.uniform_values(n, dt, -1.0, 1.0, a.seed)
+    else:
+        v = mesh.uniform_values(n, dt, -(2 ** 30), 2 ** 30, a.seed)
+    return ids, v
+
+
+def cpu_reference_run(a, ids, v, warmup, steps):
+    """Oracle port of the host ogs GatherScatter on all host cores."""
+    import oracle
+    oracle.build(ref=False)
+    cores = os.cpu_count() or 1
+    oracle.set_threads(cores)
+    h = oracle.OracleOgs(ids.copy(), "unsigned")
+    x = v.copy()
+    for _ in range(warmup):
+        h.gather_scatter(x, a.k, a.op, "sym")
+    times = []
+    for _ in range(steps):
+        np.copyto(x, v)
+        t0 = time.perf_counter()
+        h.gather_scatter(x, a.k, a.op, "sym")
+        times.append(time.perf_counter() - t0)
+    return h, times, cores
+
+
+# ------------------------------------------------------------------ arms
+def run_reference(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    ids, v = make_inputs(a)
+    h, times, cores = cpu_reference_run(a, ids, v, a.warmup, a.steps)
+    t = sum(times) / len(times)
+    value = h.NgatherGlobal / t
+    line = {
+        "metric": "fp64 GatherScatter DOFS/s" if a.dtype == "float64" else f"{a.dtype} GatherScatter DOFS/s",
+        "value": value, "unit": "DOFS/s", "impl": "reference", "n_gpus": a.gpus, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": {"float64": "f64", "float32": "f32", "int32": "i32", "int64": "i64"}[a.dtype],
+        "data": "synthetic (MakeIds box mesh, seeded U[-1,1])",
+        "config": {"workload": workload_name(a), "local_dofs": int(ids.size),
+                   "global_dofs": int(h.NgatherGlobal), "k": a.k, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "DOFS/s", "cores": cores, "kind": "port",
+                         "sample": f"{a.steps} full GatherScatter calls after {a.warmup} warm-up, "
+                                   f"OpenMP over {cores} threads"},
+        "e2e": {"value": value, "unit": "DOFS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(a):
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from dawgs_gb300 import _lib, ogs
+    ids, v = make_inputs(a)
+    g = ogs.ogs_t().Setup(ids.size, ids.copy(), None, ogs.Unsigned, ogs.Auto, False)
+    tcode, ocode = TYPE_CODE[a.dtype], OP_CODE[a.op]
+    s = np.dtype(a.dtype).itemsize
+    pristine = torch.from_numpy(v).to(dev)
+    work = pristine.clone()
+    l2 = torch.cuda.get_device_properties(dev).L2_cache_size
+    flush = torch.empty(2 * l2 // 4 + 1, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    L = _lib.lib()
+    h = g.handle
+
+    def step(ev0=None, ev1=None):
+        if ev0 is not None:
+            ev0.record(stream)
+        st = L.ogs_gather_scatter(h, work.data_ptr(), a.k, tcode, ocode, 0, stream.cuda_stream)
+        if ev1 is not None:
+            ev1.record(stream)
+        if st:
+            _lib.check(st)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    for _ in range(a.warmup):
+        work.copy_(pristine)
+        flush.zero_()
+        step()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    with Clocks(local) as clk:
+        barrier()
+        w0 = time.perf_counter()
+        for e0, e1 in evs:
+            work.copy_(pristine)
+            flush.zero_()
+            step(e0, e1)
+        barrier()
+        w1 = time.perf_counter()
+    kt = [e0.elapsed_time(e1) * 1e-3 for e0, e1 in evs]
+    t_kernel = sum(kt)
+    if world > 1:
+        tt = torch.tensor([t_kernel], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_kernel = float(tt.item())
+    per_step = t_kernel / a.steps
+    value = world * g.NgatherGlobal * a.steps / t_kernel
+
+    # e2e through the C ABI host-buffer entry point, pinned host memory
+    e2e = None
+    if not a.no_e2e:
+        host = torch.from_numpy(v.copy()).pin_memory()
+        for _ in range(3):
+            host.copy_(torch.from_numpy(v))
+            _lib.check(L.ogs_gather_scatter_host(h, host.data_ptr(), a.k, tcode, ocode, 0, stream.cuda_stream))
+        et = []
+        for _ in range(a.steps):
+            host.copy_(torch.from_numpy(v))
+            flush.zero_()
+            barrier()
+            t0 = time.perf_counter()
+            _lib.check(L.ogs_gather_scatter_host(h, host.data_ptr(), a.k, tcode, ocode, 0, stream.cuda_stream))
+            et.append(time.perf_counter() - t0)
+        t_e2e = sum(et)
+        if world > 1:
+            tt = torch.tensor([t_e2e], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t_e2e = float(tt.item())
+        nbytes = a.k * ids.size * s
+        e2e = {"value": world * g.NgatherGlobal * a.steps / t_e2e, "unit": "DOFS/s",
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "ms_per_step": 1e3 * t_e2e / a.steps, "api": "ogs_gather_scatter_host (C ABI)"}
+
+    # correctness of the timed configuration on this run's own output
+    work.copy_(pristine)
+    step()
+    torch.cuda.synchronize(dev)
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        hc, times, cores = cpu_reference_run(a, ids, v, 2, 5)
+        x = v.copy()
+        hc.gather_scatter(x, a.k, a.op, "sym")
+        got = work.cpu().numpy()
+        if got.tobytes() != x.tobytes():
+            raise SystemExit("bench: GPU result differs from the oracle on the timed workload")
+        tc = sum(times) / len(times)
+        cpu = {"value": hc.NgatherGlobal / tc, "unit": "DOFS/s", "cores": cores, "kind": "port",
+               "sample": f"5 full GatherScatter calls on this workload after 2 warm-up, OpenMP over {cores} "
+                         "threads; its output is also compared bit for bit with the GPU result"}
+
+    peak, peak_src = hbm_peak()
+    nbytes_alg = alg_bytes(ids.size, g.nnzT, g.NlocalT, a.k, s)
+    achieved = nbytes_alg / per_step / 1e9
+    stats = g.layout_stats()
+    line = {
+        "metric": "fp64 GatherScatter DOFS/s" if a.dtype == "float64" else f"{a.dtype} GatherScatter DOFS/s",
+        "value": value, "unit": "DOFS/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": {"float64": "f64", "float32": "f32", "int32": "i32", "int64": "i64"}[a.dtype],
+        "data": "synthetic (MakeIds box mesh, seeded U[-1,1])",
+        "config": {"workload": workload_name(a), "local_dofs": int(ids.size),
+                   "global_dofs": int(g.NgatherGlobal), "k": a.k,
+                   "l2": f"flushed between steps ({flush.numel() * 4 >> 20} MiB write)",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "tiles": stats["ntiles"]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": profiled_traffic(),
+                     "alg_bytes_per_launch": nbytes_alg, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"
+                     if peak_src == "measured" else "fallback 6.8 TB/s"},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": a.steps,
+        "clocks": clk.summary(),
+        "wall_ms_per_step_incl_restore_and_flush": 1e3 * (w1 - w0) / a.steps,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return run_reference(a)
+    return run_ours(a)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

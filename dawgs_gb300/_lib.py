@@ -1,0 +1,81 @@
+"""ctypes binding of libdawgs_ogs.so, the C ABI declared in include/ogs_c.h.
+
+The library must have been built (``python -m dawgs_gb300.build`` or
+``__graft_entry__.build()``); there is no fallback implementation, so a missing
+library is an ImportError-style failure at first use.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from .build import LIB
+
+OGS_OK, OGS_EINVAL, OGS_ENOMEM, OGS_EDEVICE, OGS_ETIMEOUT, OGS_ERANGE, OGS_EUNDEFINED = range(7)
+STATUS_NAMES = {0: "OGS_OK", 1: "OGS_EINVAL", 2: "OGS_ENOMEM", 3: "OGS_EDEVICE",
+                4: "OGS_ETIMEOUT", 5: "OGS_ERANGE", 6: "OGS_EUNDEFINED"}
+
+SETUP_VERBOSE = 1
+SETUP_HOST_ONLY = 2
+
+# every symbol include/ogs_c.h declares: (name, restype, argtypes)
+_vp, _i, _i64, _u = C.c_void_p, C.c_int, C.c_int64, C.c_uint
+SIGNATURES = {
+    "ogs_setup": (_i, [C.POINTER(_vp), _i64, _vp, _i, _i, _i, _i]),
+    "ogs_setup_ex": (_i, [C.POINTER(_vp), _i64, _vp, _i, _i, _u]),
+    "ogs_free": (_i, [_vp]),
+    "ogs_gather_scatter": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),
+    "ogs_gather_scatter_many": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),
+    "ogs_gather": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _vp]),
+    "ogs_scatter": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp]),
+    "ogs_gather_scatter_host": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),
+    "ogs_gather_host": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _vp]),
+    "ogs_scatter_host": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp]),
+    "ogs_get_counts": (_i, [_vp, _vp]),
+    "ogs_get_maps": (_i, [_vp, _vp, _vp, _vp, _vp]),
+    "ogs_get_layout_stats": (_i, [_vp, _vp]),
+    "ogs_last_error_string": (C.c_char_p, []),
+    "ogs_version": (_i, []),
+}
+
+
+class OgsCounts(C.Structure):
+    _fields_ = [("N", C.c_int64), ("Ngather", C.c_int64), ("NgatherGlobal", C.c_int64),
+                ("NlocalP", C.c_int64), ("NlocalT", C.c_int64), ("nnzT", C.c_int64),
+                ("nnzN", C.c_int64), ("gather_defined", C.c_int32), ("kind", C.c_int32),
+                ("unique", C.c_int32), ("max_degree", C.c_int32)]
+
+
+class OgsLayoutStats(C.Structure):
+    _fields_ = [("rows_by_degree", C.c_int64 * 9), ("nnz_general", C.c_int64),
+                ("ntiles", C.c_int64), ("device_bytes", C.c_int64)]
+
+
+class OgsError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise ImportError(f"{LIB} is missing: build it with `python -m dawgs_gb300.build`; "
+                              "the gather-scatter path has no CPU fallback")
+        L = C.CDLL(LIB)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != OGS_OK:
+        raise OgsError(status, lib().ogs_last_error_string().decode())

@@ -1,0 +1,353 @@
+// ogs_capi.cpp -- the C ABI (include/ogs_c.h): argument checks, the mapping of
+// (kind, Transpose) to the members each operation reads and writes, and the
+// host-buffer entry points.  No exception crosses this boundary.
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "ogs_internal.hpp"
+
+namespace ogsgb {
+
+static thread_local std::string g_last_error;
+
+ogs_status set_error(ogs_status s, const std::string& msg) {
+  g_last_error = msg;
+  return s;
+}
+
+namespace {
+
+size_t type_size(int type) { return (type == OGS_DOUBLE || type == OGS_INT64) ? 8 : 4; }
+
+ogs_status check_common(ogs_handle h, int k, int type, int trans, const char* fn) {
+  if (!h) return set_error(OGS_EINVAL, std::string(fn) + ": handle is NULL");
+  if (h->host_only) return set_error(OGS_EINVAL, std::string(fn) + ": handle was set up host-only");
+  if (k < 1) return set_error(OGS_EINVAL, std::string(fn) + ": k must be >= 1");
+  if (type < OGS_FLOAT || type > OGS_INT64) return set_error(OGS_EINVAL, std::string(fn) + ": unknown type");
+  if (trans < OGS_SYM || trans > OGS_TRANS) return set_error(OGS_EINVAL, std::string(fn) + ": unknown transpose");
+  if (h->N > 0) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(OGS_EDEVICE, std::string(fn) + ": " + cudaGetErrorString(e));
+    if (dev != h->device)
+      return set_error(OGS_EINVAL, std::string(fn) + ": handle lives on device " + std::to_string(h->device) +
+                                       ", current device is " + std::to_string(dev));
+  }
+  return OGS_OK;
+}
+
+ogs_status check_op(int op, const char* fn) {
+  if (op < OGS_ADD || op > OGS_MIN) return set_error(OGS_EINVAL, std::string(fn) + ": unknown op");
+  return OGS_OK;
+}
+
+// Members read and written, ogsOperator.cpp:71-79 (Gather), 214-222 (Scatter),
+// 321-339 (GatherScatter).  Unsigned handles alias N to T, so every transpose
+// acts as Sym there.
+Pattern pattern_for(const ogs_handle_s* h, int mode, int trans) {
+  Pattern p{0, 0, 0};
+  if (h->kind != OGS_SIGNED) return p;
+  if (mode == kModeGS) {
+    if (trans == OGS_TRANS) p = Pattern{0, 1, 1};
+    else if (trans == OGS_NOTRANS) p = Pattern{1, 0, 0};
+  } else if (mode == kModeGather) {
+    if (trans == OGS_NOTRANS) p = Pattern{1, 0, 1};
+  } else {
+    if (trans == OGS_TRANS) p = Pattern{0, 1, 1};
+  }
+  return p;
+}
+
+ogs_status launch(const ogs_handle_s* h, const FieldArgs& f, int mode, int op, Pattern pat, int type,
+                  void* stream, const char* fn) {
+  int e = 0;
+  switch (type) {
+    case OGS_FLOAT: e = launch_f32(h->dmaps, f, mode, op, pat, stream); break;
+    case OGS_DOUBLE: e = launch_f64(h->dmaps, f, mode, op, pat, stream); break;
+    case OGS_INT32: e = launch_i32(h->dmaps, f, mode, op, pat, stream); break;
+    default: e = launch_i64(h->dmaps, f, mode, op, pat, stream); break;
+  }
+  if (e != 0)
+    return set_error(OGS_EDEVICE, std::string(fn) + ": kernel launch failed: " +
+                                      cudaGetErrorString(static_cast<cudaError_t>(e)));
+  return OGS_OK;
+}
+
+ogs_status ensure_stage(ogs_handle_s* h, size_t bytes, const char* fn) {
+  if (bytes <= h->stage_bytes) return OGS_OK;
+  if (h->stage) cudaFree(h->stage);
+  h->stage = nullptr;
+  h->stage_bytes = 0;
+  cudaError_t e = cudaMalloc(&h->stage, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    h->stage = nullptr;
+    return set_error(e == cudaErrorMemoryAllocation ? OGS_ENOMEM : OGS_EDEVICE,
+                     std::string(fn) + ": staging allocation: " + cudaGetErrorString(e));
+  }
+  h->stage_bytes = bytes;
+  return OGS_OK;
+}
+
+ogs_status cuda_status(cudaError_t e, const char* fn, const char* what) {
+  if (e == cudaSuccess) return OGS_OK;
+  return set_error(OGS_EDEVICE, std::string(fn) + ": " + what + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace
+}  // namespace ogsgb
+
+using namespace ogsgb;
+
+extern "C" {
+
+const char* ogs_last_error_string(void) { return g_last_error.c_str(); }
+
+int ogs_version(void) { return 10000; }
+
+ogs_status ogs_setup_ex(ogs_handle* out, int64_t N, int64_t* ids, int kind, int unique, unsigned flags) {
+  if (!out) return set_error(OGS_EINVAL, "ogs_setup: out is NULL");
+  *out = nullptr;
+  const auto t0 = std::chrono::steady_clock::now();
+  ogs_handle_s* h = new (std::nothrow) ogs_handle_s();
+  if (!h) return set_error(OGS_ENOMEM, "ogs_setup: out of host memory");
+  try {
+    ogs_status s = build_host_maps(h, N, ids, kind, unique);
+    if (s != OGS_OK) { delete h; return s; }
+    build_layout(h);
+    h->host_only = (flags & OGS_SETUP_HOST_ONLY) != 0;
+    if (!h->host_only) {
+      s = upload_layout(h);
+      if (s != OGS_OK) { release_device(h); delete h; return s; }
+      cudaError_t e = cudaDeviceSynchronize();
+      if (e != cudaSuccess) {
+        release_device(h);
+        delete h;
+        return cuda_status(e, "ogs_setup", "synchronize");
+      }
+    }
+  } catch (const std::bad_alloc&) {
+    delete h;
+    return set_error(OGS_ENOMEM, "ogs_setup: out of host memory");
+  }
+  if (flags & OGS_SETUP_VERBOSE) {  // ogsSetup.cpp:184-189
+    const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::printf("ogs Setup Time: %g seconds.\n", dt);
+  }
+  *out = h;
+  return OGS_OK;
+}
+
+ogs_status ogs_setup(ogs_handle* out, int64_t N, int64_t* ids, int kind, int method, int unique,
+                     int verbose) {
+  if (method < OGS_AUTO || method > OGS_ALLTOALL) return set_error(OGS_EINVAL, "ogs_setup: unknown method");
+  return ogs_setup_ex(out, N, ids, kind, unique, verbose ? OGS_SETUP_VERBOSE : 0u);
+}
+
+ogs_status ogs_free(ogs_handle h) {
+  if (!h) return OGS_OK;
+  release_device(h);
+  delete h;
+  return OGS_OK;
+}
+
+ogs_status ogs_gather_scatter(ogs_handle h, void* d_v, int k, int type, int op, int trans, void* stream) {
+  const char* fn = "ogs_gather_scatter";
+  ogs_status s = check_common(h, k, type, trans, fn);
+  if (s == OGS_OK) s = check_op(op, fn);
+  if (s != OGS_OK) return s;
+  if (h->N == 0) return OGS_OK;
+  if (!d_v) return set_error(OGS_EINVAL, "ogs_gather_scatter: d_v is NULL");
+  FieldArgs f{};
+  f.v = d_v;
+  f.K = k;
+  return launch(h, f, kModeGS, op, pattern_for(h, kModeGS, trans), type, stream, fn);
+}
+
+ogs_status ogs_gather_scatter_many(ogs_handle h, void* const* d_vs, int k, int type, int op, int trans,
+                                   void* stream) {
+  const char* fn = "ogs_gather_scatter_many";
+  ogs_status s = check_common(h, k, type, trans, fn);
+  if (s == OGS_OK) s = check_op(op, fn);
+  if (s != OGS_OK) return s;
+  if (h->N == 0) return OGS_OK;
+  if (!d_vs) return set_error(OGS_EINVAL, "ogs_gather_scatter_many: d_vs is NULL");
+  const Pattern pat = pattern_for(h, kModeGS, trans);
+  for (int k0 = 0; k0 < k; k0 += kMaxMany) {
+    FieldArgs f{};
+    f.is_many = 1;
+    f.K = (k - k0 < kMaxMany) ? (k - k0) : kMaxMany;
+    for (int j = 0; j < f.K; ++j) {
+      if (!d_vs[k0 + j]) return set_error(OGS_EINVAL, "ogs_gather_scatter_many: a field pointer is NULL");
+      f.many[j] = d_vs[k0 + j];
+    }
+    s = launch(h, f, kModeGS, op, pat, type, stream, fn);
+    if (s != OGS_OK) return s;
+  }
+  return OGS_OK;
+}
+
+ogs_status ogs_gather(ogs_handle h, void* d_gv, const void* d_v, int k, int type, int op, int trans,
+                      void* stream) {
+  const char* fn = "ogs_gather";
+  ogs_status s = check_common(h, k, type, trans, fn);
+  if (s == OGS_OK) s = check_op(op, fn);
+  if (s != OGS_OK) return s;
+  if (!h->gather_defined)  // ogsSetup.cpp:861-864
+    return set_error(OGS_EUNDEFINED, "Gather operation not well-defined.");
+  if (h->N == 0 || h->NlocalT == 0) return OGS_OK;
+  if (!d_gv || !d_v) return set_error(OGS_EINVAL, "ogs_gather: NULL buffer");
+  FieldArgs f{};
+  f.v = const_cast<void*>(d_v);
+  f.gv = d_gv;
+  f.K = k;
+  return launch(h, f, kModeGather, op, pattern_for(h, kModeGather, trans), type, stream, fn);
+}
+
+ogs_status ogs_scatter(ogs_handle h, void* d_v, const void* d_gv, int k, int type, int trans, void* stream) {
+  const char* fn = "ogs_scatter";
+  ogs_status s = check_common(h, k, type, trans, fn);
+  if (s != OGS_OK) return s;
+  if (!h->gather_defined)  // AssertGatherDefined in ScatterStart, ogs.cpp:398
+    return set_error(OGS_EUNDEFINED, "Gather operation not well-defined.");
+  if (h->N == 0 || h->NlocalT == 0) return OGS_OK;
+  if (!d_gv || !d_v) return set_error(OGS_EINVAL, "ogs_scatter: NULL buffer");
+  FieldArgs f{};
+  f.v = d_v;
+  f.gv = const_cast<void*>(d_gv);
+  f.K = k;
+  return launch(h, f, kModeScatter, OGS_ADD, pattern_for(h, kModeScatter, trans), type, stream, fn);
+}
+
+ogs_status ogs_gather_scatter_host(ogs_handle h, void* v, int k, int type, int op, int trans, void* stream) {
+  const char* fn = "ogs_gather_scatter_host";
+  ogs_status s = check_common(h, k, type, trans, fn);
+  if (s == OGS_OK) s = check_op(op, fn);
+  if (s != OGS_OK) return s;
+  if (h->N == 0) return OGS_OK;
+  if (!v) return set_error(OGS_EINVAL, "ogs_gather_scatter_host: v is NULL");
+  const size_t bytes = static_cast<size_t>(h->N) * k * type_size(type);
+  if ((s = ensure_stage(h, bytes, fn)) != OGS_OK) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if ((s = cuda_status(cudaMemcpyAsync(h->stage, v, bytes, cudaMemcpyHostToDevice, st), fn, "copy in")) != OGS_OK)
+    return s;
+  FieldArgs f{};
+  f.v = h->stage;
+  f.K = k;
+  if ((s = launch(h, f, kModeGS, op, pattern_for(h, kModeGS, trans), type, stream, fn)) != OGS_OK) return s;
+  if ((s = cuda_status(cudaMemcpyAsync(v, h->stage, bytes, cudaMemcpyDeviceToHost, st), fn, "copy out")) != OGS_OK)
+    return s;
+  return cuda_status(cudaStreamSynchronize(st), fn, "synchronize");
+}
+
+ogs_status ogs_gather_host(ogs_handle h, void* gv, const void* v, int k, int type, int op, int trans,
+                           void* stream) {
+  const char* fn = "ogs_gather_host";
+  ogs_status s = check_common(h, k, type, trans, fn);
+  if (s == OGS_OK) s = check_op(op, fn);
+  if (s != OGS_OK) return s;
+  if (!h->gather_defined) return set_error(OGS_EUNDEFINED, "Gather operation not well-defined.");
+  if (h->N == 0 || h->NlocalT == 0) return OGS_OK;
+  if (!gv || !v) return set_error(OGS_EINVAL, "ogs_gather_host: NULL buffer");
+  const size_t ts = type_size(type);
+  const size_t vb = static_cast<size_t>(h->N) * k * ts;
+  const size_t voff = (vb + 255) / 256 * 256;
+  const size_t gb = static_cast<size_t>(h->NlocalT) * k * ts;
+  if ((s = ensure_stage(h, voff + gb, fn)) != OGS_OK) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* base = static_cast<char*>(h->stage);
+  if ((s = cuda_status(cudaMemcpyAsync(base, v, vb, cudaMemcpyHostToDevice, st), fn, "copy in")) != OGS_OK)
+    return s;
+  FieldArgs f{};
+  f.v = base;
+  f.gv = base + voff;
+  f.K = k;
+  if ((s = launch(h, f, kModeGather, op, pattern_for(h, kModeGather, trans), type, stream, fn)) != OGS_OK)
+    return s;
+  const size_t ob = static_cast<size_t>(trans == OGS_NOTRANS ? h->NlocalP : h->NlocalT) * k * ts;
+  if ((s = cuda_status(cudaMemcpyAsync(gv, base + voff, ob, cudaMemcpyDeviceToHost, st), fn, "copy out")) != OGS_OK)
+    return s;
+  return cuda_status(cudaStreamSynchronize(st), fn, "synchronize");
+}
+
+ogs_status ogs_scatter_host(ogs_handle h, void* v, const void* gv, int k, int type, int trans, void* stream) {
+  const char* fn = "ogs_scatter_host";
+  ogs_status s = check_common(h, k, type, trans, fn);
+  if (s != OGS_OK) return s;
+  if (!h->gather_defined) return set_error(OGS_EUNDEFINED, "Gather operation not well-defined.");
+  if (h->N == 0 || h->NlocalT == 0) return OGS_OK;
+  if (!gv || !v) return set_error(OGS_EINVAL, "ogs_scatter_host: NULL buffer");
+  const size_t ts = type_size(type);
+  const size_t vb = static_cast<size_t>(h->N) * k * ts;
+  const size_t voff = (vb + 255) / 256 * 256;
+  const size_t gb = static_cast<size_t>(h->NlocalT) * k * ts;
+  if ((s = ensure_stage(h, voff + gb, fn)) != OGS_OK) return s;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* base = static_cast<char*>(h->stage);
+  const Pattern pat = pattern_for(h, kModeScatter, trans);
+  // Entries outside the map keep their values, so v goes in unless the
+  // scatter overwrites every entry.
+  const bool writes_all = h->covers_all && !pat.scatter_n;
+  if (!writes_all &&
+      (s = cuda_status(cudaMemcpyAsync(base, v, vb, cudaMemcpyHostToDevice, st), fn, "copy in v")) != OGS_OK)
+    return s;
+  const size_t ib = static_cast<size_t>(trans == OGS_TRANS ? h->NlocalP : h->NlocalT) * k * ts;
+  if ((s = cuda_status(cudaMemcpyAsync(base + voff, gv, ib, cudaMemcpyHostToDevice, st), fn, "copy in gv")) !=
+      OGS_OK)
+    return s;
+  FieldArgs f{};
+  f.v = base;
+  f.gv = base + voff;
+  f.K = k;
+  if ((s = launch(h, f, kModeScatter, OGS_ADD, pat, type, stream, fn)) != OGS_OK) return s;
+  if ((s = cuda_status(cudaMemcpyAsync(v, base, vb, cudaMemcpyDeviceToHost, st), fn, "copy out")) != OGS_OK)
+    return s;
+  return cuda_status(cudaStreamSynchronize(st), fn, "synchronize");
+}
+
+ogs_status ogs_get_counts(ogs_handle h, ogs_counts* out) {
+  if (!h || !out) return set_error(OGS_EINVAL, "ogs_get_counts: NULL argument");
+  out->N = h->N;
+  out->Ngather = h->Ngather;
+  out->NgatherGlobal = h->NgatherGlobal;
+  out->NlocalP = h->NlocalP;
+  out->NlocalT = h->NlocalT;
+  out->nnzT = h->nnzT;
+  out->nnzN = h->nnzN;
+  out->gather_defined = h->gather_defined;
+  out->kind = h->kind;
+  out->unique = h->unique;
+  out->max_degree = h->max_degree;
+  return OGS_OK;
+}
+
+ogs_status ogs_get_maps(ogs_handle h, int32_t* rowStartsT, int32_t* colIdsT, int32_t* rowStartsN,
+                        int32_t* colIdsN) {
+  if (!h) return set_error(OGS_EINVAL, "ogs_get_maps: handle is NULL");
+  const bool sgn = h->kind == OGS_SIGNED;
+  const std::vector<int32_t>& rsN = sgn ? h->rowStartsN : h->rowStartsT;
+  const std::vector<int32_t>& ciN = sgn ? h->colIdsN : h->colIdsT;
+  if (rowStartsT) std::memcpy(rowStartsT, h->rowStartsT.data(), h->rowStartsT.size() * 4);
+  if (colIdsT && !h->colIdsT.empty()) std::memcpy(colIdsT, h->colIdsT.data(), h->colIdsT.size() * 4);
+  if (rowStartsN) std::memcpy(rowStartsN, rsN.data(), rsN.size() * 4);
+  if (colIdsN && !ciN.empty()) std::memcpy(colIdsN, ciN.data(), ciN.size() * 4);
+  return OGS_OK;
+}
+
+ogs_status ogs_get_layout_stats(ogs_handle h, ogs_layout_stats* out) {
+  if (!h || !out) return set_error(OGS_EINVAL, "ogs_get_layout_stats: NULL argument");
+  std::memset(out, 0, sizeof(*out));
+  for (int d = 1; d <= kDmax; ++d) out->rows_by_degree[d] = static_cast<int64_t>(h->lay.rows[d].size());
+  out->rows_by_degree[0] = static_cast<int64_t>(h->lay.g_rows.size());
+  out->nnz_general = static_cast<int64_t>(h->lay.g_colsT.size());
+  out->ntiles = static_cast<int64_t>(h->lay.tiles.size());
+  out->device_bytes = static_cast<int64_t>(h->arena_bytes);
+  return OGS_OK;
+}
+
+}  // extern "C"

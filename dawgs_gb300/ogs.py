@@ -1,0 +1,230 @@
+"""Python mirror of libParanumal's ``ogs::ogs_t`` (include/ogs.hpp:216-345 of
+the reference) over the C ABI of libdawgs_ogs.so.
+
+Names, argument order and meaning follow the reference::
+
+    g = ogs_t()
+    g.Setup(N, ids, comm, Unsigned, Auto, unique=False, verbose=False, platform=None)
+    g.GatherScatter(o_v, k, Add, Sym)     # torch CUDA tensor: runs on its stream
+    g.GatherScatter(v, k, Add, Sym)       # host buffer (numpy / CPU tensor): copied
+                                          # through the GPU and back
+    g.Gather(o_gv, o_v, k, Add, Trans)
+    g.Scatter(o_v, o_gv, k, NoTrans)
+
+Errors raise ``OgsError`` with the library's status and message, where the
+reference raises ``libp::exception`` through LIBP_ABORT.  ``comm``, ``method``
+and ``platform`` are accepted and ignored: the path runs at one rank.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+
+import numpy as np
+
+from . import _lib
+from ._lib import OgsCounts, OgsError, OgsLayoutStats, check, lib
+
+
+class Type(enum.IntEnum):  # include/ogs.hpp:179
+    Float = 0
+    Double = 1
+    Int32 = 2
+    Int64 = 3
+
+
+class Op(enum.IntEnum):  # include/ogs.hpp:186
+    Add = 0
+    Mul = 1
+    Max = 2
+    Min = 3
+
+
+class Transpose(enum.IntEnum):  # include/ogs.hpp:189
+    Sym = 0
+    NoTrans = 1
+    Trans = 2
+
+
+class Method(enum.IntEnum):  # include/ogs.hpp:192
+    Auto = 0
+    Pairwise = 1
+    CrystalRouter = 2
+    AllToAll = 3
+
+
+class Kind(enum.IntEnum):  # include/ogs.hpp:195
+    Unsigned = 0
+    Signed = 1
+    Halo = 2
+
+
+Float, Double, Int32, Int64 = Type
+Add, Mul, Max, Min = Op
+Sym, NoTrans, Trans = Transpose
+Auto, Pairwise, CrystalRouter, AllToAll = Method
+Unsigned, Signed, Halo = Kind
+
+_NP_TYPES = {np.dtype(np.float32): Float, np.dtype(np.float64): Double,
+             np.dtype(np.int32): Int32, np.dtype(np.int64): Int64}
+
+
+def _type_of(buf) -> Type:
+    if isinstance(buf, np.ndarray):
+        t = _NP_TYPES.get(buf.dtype)
+    else:
+        import torch
+        t = {torch.float32: Float, torch.float64: Double,
+             torch.int32: Int32, torch.int64: Int64}.get(buf.dtype)
+    if t is None:
+        raise OgsError(_lib.OGS_EINVAL, f"unsupported field dtype {buf.dtype}")
+    return t
+
+
+def _is_device(buf) -> bool:
+    return not isinstance(buf, np.ndarray) and getattr(buf, "is_cuda", False)
+
+
+def _ptr(buf) -> int:
+    if isinstance(buf, np.ndarray):
+        if not buf.flags.c_contiguous:
+            raise OgsError(_lib.OGS_EINVAL, "field buffers must be contiguous")
+        return buf.ctypes.data
+    if not buf.is_contiguous():
+        raise OgsError(_lib.OGS_EINVAL, "field buffers must be contiguous")
+    return buf.data_ptr()
+
+
+def _stream_of(stream):
+    if stream is not None:
+        return getattr(stream, "cuda_stream", stream)
+    import torch
+    if torch.cuda.is_available():
+        return torch.cuda.current_stream().cuda_stream
+    return None
+
+
+class ogs_t:
+    """One single-rank gather-scatter handle (ogs::ogs_t)."""
+
+    def __init__(self, platform=None):
+        self._h = None
+        self.N = self.Ngather = self.NgatherGlobal = self.NlocalT = self.NlocalP = 0
+        self.NhaloT = self.NhaloP = 0
+        self.nnzT = self.nnzN = 0
+        self.gather_defined = False
+        self.unique = False
+        self.kind = Unsigned
+        self.max_degree = 0
+
+    # ogs_t::Setup, include/ogs.hpp:221-228 / libs/ogs/ogsSetup.cpp:44-53
+    def Setup(self, N, ids, comm=None, kind=Unsigned, method=Auto, unique=False,
+              verbose=False, platform=None, host_only=False):
+        self.Free()
+        if not (isinstance(ids, np.ndarray) and ids.dtype == np.int64 and ids.flags.c_contiguous):
+            raise OgsError(_lib.OGS_EINVAL, "ids must be a contiguous int64 numpy array")
+        if len(ids) < N:
+            raise OgsError(_lib.OGS_EINVAL, "ids is shorter than N")
+        h = C.c_void_p()
+        flags = (_lib.SETUP_VERBOSE if verbose else 0) | (_lib.SETUP_HOST_ONLY if host_only else 0)
+        check(lib().ogs_setup_ex(C.byref(h), int(N), ids.ctypes.data, int(kind), int(bool(unique)), flags))
+        self._h = h
+        c = OgsCounts()
+        check(lib().ogs_get_counts(h, C.byref(c)))
+        self.N, self.Ngather, self.NgatherGlobal = c.N, c.Ngather, c.NgatherGlobal
+        self.NlocalP, self.NlocalT = c.NlocalP, c.NlocalT
+        self.nnzT, self.nnzN = c.nnzT, c.nnzN
+        self.gather_defined = bool(c.gather_defined)
+        self.kind, self.unique, self.max_degree = Kind(c.kind), bool(c.unique), c.max_degree
+        return self
+
+    def Free(self):
+        if self._h is not None and _lib._lib is not None:
+            lib().ogs_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.Free()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise OgsError(_lib.OGS_EINVAL, "ogs handle is not set up")
+        return self._h
+
+    # ---- GatherScatter (include/ogs.hpp:232-265) ----
+    def GatherScatter(self, v, k, op=Add, trans=Sym, stream=None):
+        t = _type_of(v)
+        if _is_device(v):
+            check(lib().ogs_gather_scatter(self.handle, _ptr(v), int(k), int(t), int(op), int(trans),
+                                           _stream_of(stream)))
+        else:
+            check(lib().ogs_gather_scatter_host(self.handle, _ptr(v), int(k), int(t), int(op),
+                                                int(trans), _stream_of(stream)))
+        return v
+
+    GatherScatterStart = GatherScatter
+
+    def GatherScatterFinish(self, v, k, op=Add, trans=Sym, stream=None):
+        return v
+
+    def GatherScatterMany(self, vs, op=Add, trans=Sym, stream=None):
+        """k separate device arrays (gslib's gs_many layout)."""
+        t = _type_of(vs[0])
+        arr = (C.c_void_p * len(vs))(*[_ptr(x) for x in vs])
+        check(lib().ogs_gather_scatter_many(self.handle, arr, len(vs), int(t), int(op), int(trans),
+                                            _stream_of(stream)))
+        return vs
+
+    # ---- Gather (include/ogs.hpp:268-306) ----
+    def Gather(self, gv, v, k, op=Add, trans=Trans, stream=None):
+        t = _type_of(v)
+        if _type_of(gv) != t:
+            raise OgsError(_lib.OGS_EINVAL, "gv and v must have the same dtype")
+        if _is_device(v) != _is_device(gv):
+            raise OgsError(_lib.OGS_EINVAL, "gv and v must both be device or both be host buffers")
+        fn = lib().ogs_gather if _is_device(v) else lib().ogs_gather_host
+        check(fn(self.handle, _ptr(gv), _ptr(v), int(k), int(t), int(op), int(trans), _stream_of(stream)))
+        return gv
+
+    GatherStart = Gather
+
+    def GatherFinish(self, gv, v, k, op=Add, trans=Trans, stream=None):
+        return gv
+
+    # ---- Scatter (include/ogs.hpp:309-341) ----
+    def Scatter(self, v, gv, k, trans=NoTrans, stream=None):
+        t = _type_of(v)
+        if _type_of(gv) != t:
+            raise OgsError(_lib.OGS_EINVAL, "gv and v must have the same dtype")
+        if _is_device(v) != _is_device(gv):
+            raise OgsError(_lib.OGS_EINVAL, "gv and v must both be device or both be host buffers")
+        fn = lib().ogs_scatter if _is_device(v) else lib().ogs_scatter_host
+        check(fn(self.handle, _ptr(v), _ptr(gv), int(k), int(t), int(trans), _stream_of(stream)))
+        return v
+
+    ScatterStart = Scatter
+
+    def ScatterFinish(self, v, gv, k, trans=NoTrans, stream=None):
+        return v
+
+    # ---- introspection ----
+    def maps(self):
+        """Host copies of (rowStartsT, colIdsT, rowStartsN, colIdsN)."""
+        rsT = np.zeros(self.NlocalT + 1, np.int32)
+        ciT = np.zeros(max(self.nnzT, 1), np.int32)
+        rsN = np.zeros(self.NlocalT + 1, np.int32)
+        ciN = np.zeros(max(self.nnzN, 1), np.int32)
+        check(lib().ogs_get_maps(self.handle, rsT.ctypes.data, ciT.ctypes.data, rsN.ctypes.data,
+                                 ciN.ctypes.data))
+        return rsT, ciT[: self.nnzT], rsN, ciN[: self.nnzN]
+
+    def layout_stats(self) -> dict:
+        s = OgsLayoutStats()
+        check(lib().ogs_get_layout_stats(self.handle, C.byref(s)))
+        return {"rows_by_degree": {d: int(s.rows_by_degree[d]) for d in range(1, 9) if s.rows_by_degree[d]},
+                "rows_general": int(s.rows_by_degree[0]), "nnz_general": int(s.nnz_general),
+                "ntiles": int(s.ntiles), "device_bytes": int(s.device_bytes)}

@@ -1,0 +1,141 @@
+/*
+ * ogs_c.h -- C ABI of the GB300 gather-scatter library (libdawgs_ogs.so).
+ *
+ * Drop-in for the single-rank hot path of libParanumal's ogs library as used
+ * by paranumal/dawgs: ogs::ogs_t::Setup / GatherScatter / Gather / Scatter
+ * (include/ogs.hpp:216-345 of the reference) over the CSR maps built by
+ * ogsBase_t::Setup (libs/ogs/ogsSetup.cpp:69-190) and applied by
+ * ogsOperator_t (libs/ogs/ogsOperator.cpp).  The reference exposes only C++
+ * templates; every entry point below replaces one of those calls and keeps
+ * its argument meaning.  Plain pointers and sizes only; device pointers are
+ * CUDA device addresses, `stream` is a cudaStream_t (NULL = legacy default).
+ *
+ * Errors never cross the ABI as exceptions: each call returns an ogs_status
+ * and ogs_last_error_string() gives the message of the calling thread's last
+ * failure (the reference aborts with LIBP_ABORT, include/utils.hpp:57-76).
+ *
+ * Operations are asynchronous on `stream` unless the name ends in _host.  A
+ * handle is immutable after setup, so calls on one handle from several
+ * streams are safe, except the _host calls, which share the handle's
+ * device staging buffer and must not overlap one another.
+ */
+#ifndef OGS_C_H
+#define OGS_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ogs_handle_s *ogs_handle;
+
+typedef enum {
+  OGS_OK = 0,
+  OGS_EINVAL = 1,    /* bad argument or option set */
+  OGS_ENOMEM = 2,    /* host or device allocation failed */
+  OGS_EDEVICE = 3,   /* CUDA runtime error (message in ogs_last_error_string) */
+  OGS_ETIMEOUT = 4,  /* a bounded device-side wait ran out */
+  OGS_ERANGE = 5,    /* sizes beyond 32-bit device indices or a stated limit */
+  OGS_EUNDEFINED = 6 /* Gather/Scatter on a handle whose gather is not well-defined */
+} ogs_status;
+
+/* ogs::Type, include/ogs.hpp:179 of the reference */
+typedef enum { OGS_FLOAT = 0, OGS_DOUBLE = 1, OGS_INT32 = 2, OGS_INT64 = 3 } ogs_type;
+/* ogs::Op, include/ogs.hpp:186 */
+typedef enum { OGS_ADD = 0, OGS_MUL = 1, OGS_MAX = 2, OGS_MIN = 3 } ogs_op;
+/* ogs::Transpose, include/ogs.hpp:189 */
+typedef enum { OGS_SYM = 0, OGS_NOTRANS = 1, OGS_TRANS = 2 } ogs_transpose;
+/* ogs::Method, include/ogs.hpp:192 -- accepted and ignored at one rank */
+typedef enum { OGS_AUTO = 0, OGS_PAIRWISE = 1, OGS_CRYSTALROUTER = 2, OGS_ALLTOALL = 3 } ogs_method;
+/* ogs::Kind, include/ogs.hpp:195 (Halo is not part of the single-rank path) */
+typedef enum { OGS_UNSIGNED = 0, OGS_SIGNED = 1, OGS_HALO = 2 } ogs_kind;
+
+/* setup flags for ogs_setup_ex */
+#define OGS_SETUP_VERBOSE   1u  /* print the reference's "ogs Setup Time" line */
+#define OGS_SETUP_HOST_ONLY 2u  /* build host maps only; no device memory, no ops */
+
+typedef struct {
+  int64_t N;              /* local nodes (ogsBase_t::N) */
+  int64_t Ngather;        /* positive gathered rows, NlocalP + NhaloP (ogsBase.hpp:51) */
+  int64_t NgatherGlobal;  /* = Ngather at one rank (ogsBase.hpp:56) */
+  int64_t NlocalP;        /* rows with a positive member = NrowsN */
+  int64_t NlocalT;        /* all rows = NrowsT */
+  int64_t nnzT, nnzN;     /* entries of the T and N maps */
+  int32_t gather_defined; /* 1 when every id group has exactly one positive member */
+  int32_t kind, unique;
+  int32_t max_degree;     /* largest row of the T map */
+} ogs_counts;
+
+typedef struct {
+  int64_t rows_by_degree[9]; /* [d] rows of exact degree d (1..8); [0] rows above 8 */
+  int64_t nnz_general;       /* entries in rows above degree 8 */
+  int64_t ntiles;            /* work tiles in one launch over the whole map */
+  int64_t device_bytes;      /* device memory held by the handle's maps */
+} ogs_layout_stats;
+
+/* ogs_t::Setup (include/ogs.hpp:221-228; libs/ogs/ogsSetup.cpp:69-190).
+ * ids[N] are global ids (0 = does not participate).  With unique=1 (Signed
+ * only) the ids are rewritten in place: one member of each group keeps a
+ * positive id (the member with the lowest local index), the others are
+ * negated (ogsSetup.cpp:138-141, 264-275).  Unsigned with unique=1 is
+ * rejected (ogsSetup.cpp:98-100).  method is accepted and ignored. */
+ogs_status ogs_setup(ogs_handle *out, int64_t N, int64_t *ids, int kind, int method,
+                     int unique, int verbose);
+ogs_status ogs_setup_ex(ogs_handle *out, int64_t N, int64_t *ids, int kind, int unique,
+                        unsigned flags);
+/* ogsBase_t::Free (libs/ogs/ogsSetup.cpp:849-859). NULL is accepted. */
+ogs_status ogs_free(ogs_handle h);
+
+/* ogs_t::GatherScatter(deviceMemory<T> o_v, k, op, trans)
+ * (include/ogs.hpp:244-247; libs/ogs/ogs.cpp:39-123 ->
+ * ogsOperator.cpp:311-360 semantics).  d_v holds k interleaved components
+ * per node: component c of node n at d_v[c + n*k]. */
+ogs_status ogs_gather_scatter(ogs_handle h, void *d_v, int k, int type, int op, int trans,
+                              void *stream);
+/* k separate arrays d_vs[0..k-1] of N values each (gslib's gs_many layout,
+ * 3rdParty/gslib/src/gs.c:1354; ogs itself has no counterpart). */
+ogs_status ogs_gather_scatter_many(ogs_handle h, void *const *d_vs, int k, int type, int op,
+                                   int trans, void *stream);
+/* ogs_t::Gather(deviceMemory<T> o_gv, o_v, k, op, trans) (include/ogs.hpp:285-289;
+ * libs/ogs/ogs.cpp:202-298; ogsOperator.cpp:60-97).  d_gv has k*Ngather values
+ * (Trans/Sym) -- rows NlocalP..NlocalT of an ill-defined handle are never
+ * produced because Gather requires gather_defined (ogsSetup.cpp:861-864). */
+ogs_status ogs_gather(ogs_handle h, void *d_gv, const void *d_v, int k, int type, int op,
+                      int trans, void *stream);
+/* ogs_t::Scatter(deviceMemory<T> o_v, o_gv, k, trans) (include/ogs.hpp:325-328;
+ * libs/ogs/ogs.cpp:392-488; ogsOperator.cpp:206-238). */
+ogs_status ogs_scatter(ogs_handle h, void *d_v, const void *d_gv, int k, int type, int trans,
+                       void *stream);
+
+/* Host-buffer overloads: ogs_t::GatherScatter/Gather/Scatter(memory<T> ...)
+ * (include/ogs.hpp:232-236, 268-273, 309-313).  The work runs on the GPU:
+ * the buffers are copied to a device staging area owned by the handle, the
+ * kernel runs on `stream`, results are copied back, and the call returns
+ * after `stream` has synchronised.  Pinned host memory gives full copy speed. */
+ogs_status ogs_gather_scatter_host(ogs_handle h, void *v, int k, int type, int op, int trans,
+                                   void *stream);
+ogs_status ogs_gather_host(ogs_handle h, void *gv, const void *v, int k, int type, int op,
+                           int trans, void *stream);
+ogs_status ogs_scatter_host(ogs_handle h, void *v, const void *gv, int k, int type, int trans,
+                            void *stream);
+
+/* Counts of ogsBase_t (include/ogs/ogsBase.hpp:50-58). */
+ogs_status ogs_get_counts(ogs_handle h, ogs_counts *out);
+/* Host copies of the CSR maps of ogsOperator_t (include/ogs/ogsOperator.hpp:47-57):
+ * rowStartsT/N[NlocalT+1], colIdsT[nnzT], colIdsN[nnzN].  Any pointer may be NULL. */
+ogs_status ogs_get_maps(ogs_handle h, int32_t *rowStartsT, int32_t *colIdsT,
+                        int32_t *rowStartsN, int32_t *colIdsN);
+/* Degree buckets and tiles the kernels run over (no reference counterpart). */
+ogs_status ogs_get_layout_stats(ogs_handle h, ogs_layout_stats *out);
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *ogs_last_error_string(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int ogs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OGS_C_H */

@@ -1,0 +1,80 @@
+"""The C ABI library loads without a GPU, exports every function that
+include/ogs_c.h declares, and rejects bad arguments with the documented status
+codes (the reference's LIBP_ABORT cases, ogsSetup.cpp:98-100, 861-864) before
+touching a device."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from dawgs_gb300 import _lib, ogs
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for fn in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not fn.endswith(".h"):
+            continue
+        src = open(os.path.join(ROOT, "include", fn)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names += re.findall(r"^\s*(?:const\s+)?[a-z_]+\s*\**\s*(ogs_[a-z_0-9]+)\s*\(", src, flags=re.M)
+    return names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    names = declared_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(built_lib, n), f"{n} is declared in include/ but not exported"
+    assert set(names) == set(_lib.SIGNATURES), "ctypes binding and header disagree"
+
+
+def test_version(built_lib):
+    assert built_lib.ogs_version() >= 10000
+
+
+def _setup(ids, kind=0, unique=0, flags=_lib.SETUP_HOST_ONLY):
+    h = C.c_void_p()
+    st = _lib.lib().ogs_setup_ex(C.byref(h), ids.size, ids.ctypes.data, kind, unique, flags)
+    return st, h
+
+
+def test_rejects_invalid_setups(built_lib):
+    ids = np.arange(1, 11, dtype=np.int64)
+    assert _setup(ids, kind=0, unique=1)[0] == _lib.OGS_EINVAL  # Unsigned + unique
+    assert b"Invalid ogs setup" in built_lib.ogs_last_error_string()
+    assert _setup(ids, kind=2)[0] == _lib.OGS_EINVAL  # Halo
+    assert _setup(ids, kind=7)[0] == _lib.OGS_EINVAL
+    bad = np.array([1, -(2 ** 63), 3], np.int64)
+    assert _setup(bad)[0] == _lib.OGS_ERANGE
+    h = C.c_void_p()
+    assert built_lib.ogs_setup_ex(C.byref(h), -1, None, 0, 0, _lib.SETUP_HOST_ONLY) == _lib.OGS_EINVAL
+    assert built_lib.ogs_setup_ex(C.byref(h), 5, None, 0, 0, _lib.SETUP_HOST_ONLY) == _lib.OGS_EINVAL
+    assert built_lib.ogs_setup_ex(None, 5, ids.ctypes.data, 0, 0, _lib.SETUP_HOST_ONLY) == _lib.OGS_EINVAL
+    assert built_lib.ogs_setup(C.byref(h), 10, ids.ctypes.data, 0, 9, 0, 0) == _lib.OGS_EINVAL  # method
+
+
+def test_host_only_handle_rejects_ops(built_lib):
+    ids = np.array([1, 2, 1, 3], np.int64)
+    st, h = _setup(ids)
+    assert st == _lib.OGS_OK
+    v = np.zeros(4)
+    assert built_lib.ogs_gather_scatter(h, v.ctypes.data, 1, 1, 0, 0, None) == _lib.OGS_EINVAL
+    assert b"host-only" in built_lib.ogs_last_error_string()
+    assert built_lib.ogs_free(h) == _lib.OGS_OK
+    assert built_lib.ogs_free(None) == _lib.OGS_OK
+    assert built_lib.ogs_gather_scatter(None, v.ctypes.data, 1, 1, 0, 0, None) == _lib.OGS_EINVAL
+
+
+def test_python_mirror_raises(built_lib):
+    ids = np.array([1, 2, 1, 3], np.int64)
+    with pytest.raises(_lib.OgsError) as e:
+        ogs.ogs_t().Setup(4, ids.copy(), None, ogs.Unsigned, ogs.Auto, True)
+    assert e.value.status == _lib.OGS_EINVAL
+    g = ogs.ogs_t().Setup(4, ids.copy(), host_only=True)
+    assert not g.gather_defined  # two members of group 1 are positive
+    assert (g.N, g.NlocalT, g.Ngather) == (4, 3, 3)

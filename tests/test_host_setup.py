@@ -1,0 +1,73 @@
+"""The library's host setup (ogs_setup_ex with OGS_SETUP_HOST_ONLY, no device
+needed) builds exactly the oracle's N and T maps and counts: same rows in the
+same first-appearance order, same ascending colIds, same NlocalP/NlocalT,
+gather_defined and rewritten ids.  The library groups ids with a hash table in
+one pass; the oracle sorts -- two algorithms for one contract
+(ogsSetup.cpp:69-190, 333-433, 569-776)."""
+import numpy as np
+import pytest
+
+from dawgs_gb300 import mesh, ogs
+from helpers import random_ids, signed_ids
+
+CASES = {
+    "c1_box": lambda: mesh.box_ids(10, 10, 10, 3),
+    "box_p1": lambda: mesh.box_ids(7, 5, 3, 1),
+    "box_permuted": lambda: mesh.permute_elements(mesh.box_ids(6, 5, 4, 4), 4, seed=2),
+    "random_multiplicity": lambda: random_ids(20000, 1500, seed=4, zero_frac=0.05),
+    "high_degree": lambda: random_ids(5000, 7, seed=8),  # rows of ~700 members
+    "all_zero": lambda: np.zeros(100, np.int64),
+    "empty": lambda: np.zeros(0, np.int64),
+    "single": lambda: np.array([42], np.int64),
+    "huge_ids": lambda: np.array([2 ** 62, -(2 ** 62), 3, 2 ** 40, 3, -(2 ** 40)], np.int64),
+}
+
+
+def _compare(oracle_mod, ids, kind, unique):
+    a = ids.copy()
+    b = ids.copy()
+    ref = oracle_mod.OracleOgs(a, kind, unique)
+    g = ogs.ogs_t().Setup(b.size, b, None, ogs.Signed if kind == "signed" else ogs.Unsigned,
+                          ogs.Auto, unique, False, None, host_only=True)
+    assert (g.NlocalP, g.NlocalT, g.Ngather, g.NgatherGlobal, g.nnzT, g.nnzN, g.gather_defined) == \
+        (ref.NlocalP, ref.NlocalT, ref.Ngather, ref.NgatherGlobal, ref.nnzT, ref.nnzN, ref.gather_defined)
+    for x, y in zip(g.maps(), ref.maps()):
+        assert np.array_equal(x, y)
+    assert np.array_equal(a, b)  # ids rewritten identically when unique
+    return g, ref
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_unsigned_maps_match_oracle(oracle_mod, name):
+    _compare(oracle_mod, CASES[name](), "unsigned", False)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+@pytest.mark.parametrize("unique", [False, True])
+def test_signed_maps_match_oracle(oracle_mod, name, unique):
+    ids = CASES[name]()
+    _compare(oracle_mod, signed_ids(ids, seed=6) if ids.size else ids, "signed", unique)
+
+
+def test_layout_covers_every_row(oracle_mod):
+    ids = random_ids(30000, 2000, seed=12, zero_frac=0.02)
+    g, ref = _compare(oracle_mod, ids, "unsigned", False)
+    st = g.layout_stats()
+    deg = np.diff(ref.maps()[0])
+    hist = np.bincount(deg, minlength=9)
+    for d in range(1, 9):
+        assert st["rows_by_degree"].get(d, 0) == hist[d]
+    assert st["rows_general"] == int((deg > 8).sum())
+    assert st["nnz_general"] == int(deg[deg > 8].sum())
+    assert st["device_bytes"] == 0  # host-only
+
+
+def test_c2_box_counts_match_closed_form(oracle_mod):
+    """24^3 p=7: 7,077,888 local / 4,826,809 global DOFs and the row-degree histogram."""
+    ids = mesh.box_ids(24, 24, 24, 7)
+    cf = mesh.box_counts(24, 24, 24, 7)
+    g = ogs.ogs_t().Setup(ids.size, ids, host_only=True)
+    assert g.N == cf["local"] == 7077888
+    assert g.NgatherGlobal == cf["global"] == 4826809
+    st = g.layout_stats()
+    assert st["rows_by_degree"] == cf["rows_by_degree"] == {1: 3112136, 2: 1470804, 4: 231702, 8: 12167}
