@@ -2,7 +2,9 @@
 
 The library must have been built (``python -m dawgs_gb300.build`` or
 ``__graft_entry__.build()``); there is no fallback implementation, so a missing
-library is an ImportError-style failure at first use.
+library is an ImportError-style failure at first use.  DAWGS_OGS_LIB names
+another build of the same library (for instance one compiled with other
+tile settings).
 """
 from __future__ import annotations
 
@@ -34,6 +36,12 @@ SIGNATURES = {
     "ogs_get_counts": (_i, [_vp, _vp]),
     "ogs_get_maps": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "ogs_get_layout_stats": (_i, [_vp, _vp]),
+    "ogs_batch_create": (_i, [C.POINTER(_vp), _i, _vp, _i, _u]),
+    "ogs_batch_set_fields": (_i, [_vp, _vp, _vp]),
+    "ogs_batch_gather_scatter": (_i, [_vp, _vp]),
+    "ogs_batch_tune": (_i, [_vp, _vp, _vp]),
+    "ogs_batch_items": (_i, [_vp, _vp]),
+    "ogs_batch_free": (_i, [_vp]),
     "ogs_last_error_string": (C.c_char_p, []),
     "ogs_version": (_i, []),
 }
@@ -48,7 +56,16 @@ class OgsCounts(C.Structure):
 
 class OgsLayoutStats(C.Structure):
     _fields_ = [("rows_by_degree", C.c_int64 * 9), ("nnz_general", C.c_int64),
-                ("ntiles", C.c_int64), ("device_bytes", C.c_int64)]
+                ("ntiles", C.c_int64), ("device_bytes", C.c_int64), ("nphases", C.c_int64),
+                ("phases", (C.c_int64 * 4) * 8)]
+
+
+class OgsBatchEntry(C.Structure):
+    _fields_ = [("h", C.c_void_p), ("d_v", C.c_void_p), ("k", C.c_int32), ("op", C.c_int32),
+                ("trans", C.c_int32), ("reserved", C.c_int32)]
+
+
+BATCH_GRAPH = 1
 
 
 class OgsError(RuntimeError):
@@ -64,10 +81,11 @@ def lib():
     """The loaded library (raises if it has not been built)."""
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB):
-            raise ImportError(f"{LIB} is missing: build it with `python -m dawgs_gb300.build`; "
+        path = os.environ.get("DAWGS_OGS_LIB") or LIB
+        if not os.path.exists(path):
+            raise ImportError(f"{path} is missing: build it with `python -m dawgs_gb300.build`; "
                               "the gather-scatter path has no CPU fallback")
-        L = C.CDLL(LIB)
+        L = C.CDLL(path)
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(L, name)
             fn.restype = res

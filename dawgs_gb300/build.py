@@ -65,9 +65,24 @@ def _compile(src, verbose, extra):
     return src, r.returncode, r.stdout + r.stderr, cmd
 
 
-def build(force: bool = False, verbose: bool = False, extra=()) -> str:
+def build(force: bool = False, verbose: bool = False, extra=(), build_dir=None, lib=None) -> str:
+    """Compile and link; `extra` nvcc flags, `build_dir`/`lib` redirect the
+    objects and the library (e.g. a variant built with other -D settings)."""
+    global BUILD, LIB
+    saved = BUILD, LIB
+    if build_dir:
+        BUILD = build_dir
+    if lib:
+        LIB = lib
+    try:
+        return _build(force, verbose, extra)
+    finally:
+        BUILD, LIB = saved
+
+
+def _build(force, verbose, extra):
     os.makedirs(BUILD, exist_ok=True)
-    os.makedirs(LIBDIR, exist_ok=True)
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
     hs = headers()
     srcs = sources()
     todo = [s for s in srcs if force or _stale(_obj(s), [s, *hs])]

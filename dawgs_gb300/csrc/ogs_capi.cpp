@@ -11,6 +11,10 @@
 
 #include "ogs_internal.hpp"
 
+#ifndef OGS_KERNEL
+#define OGS_KERNEL 0
+#endif
+
 namespace ogsgb {
 
 static thread_local std::string g_last_error;
@@ -63,19 +67,24 @@ Pattern pattern_for(const ogs_handle_s* h, int mode, int trans) {
   return p;
 }
 
-ogs_status launch(const ogs_handle_s* h, const FieldArgs& f, int mode, int op, Pattern pat, int type,
-                  void* stream, const char* fn) {
+ogs_status launch_maps(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, int type,
+                       void* stream, const char* fn) {
   int e = 0;
   switch (type) {
-    case OGS_FLOAT: e = launch_f32(h->dmaps, f, mode, op, pat, stream); break;
-    case OGS_DOUBLE: e = launch_f64(h->dmaps, f, mode, op, pat, stream); break;
-    case OGS_INT32: e = launch_i32(h->dmaps, f, mode, op, pat, stream); break;
-    default: e = launch_i64(h->dmaps, f, mode, op, pat, stream); break;
+    case OGS_FLOAT: e = launch_f32(m, f, mode, op, pat, stream); break;
+    case OGS_DOUBLE: e = launch_f64(m, f, mode, op, pat, stream); break;
+    case OGS_INT32: e = launch_i32(m, f, mode, op, pat, stream); break;
+    default: e = launch_i64(m, f, mode, op, pat, stream); break;
   }
   if (e != 0)
     return set_error(OGS_EDEVICE, std::string(fn) + ": kernel launch failed: " +
                                       cudaGetErrorString(static_cast<cudaError_t>(e)));
   return OGS_OK;
+}
+
+ogs_status launch(const ogs_handle_s* h, const FieldArgs& f, int mode, int op, Pattern pat, int type,
+                  void* stream, const char* fn) {
+  return launch_maps(h->dmaps, f, mode, op, pat, type, stream, fn);
 }
 
 ogs_status ensure_stage(ogs_handle_s* h, size_t bytes, const char* fn) {
@@ -97,6 +106,29 @@ ogs_status ensure_stage(ogs_handle_s* h, size_t bytes, const char* fn) {
 ogs_status cuda_status(cudaError_t e, const char* fn, const char* what) {
   if (e == cudaSuccess) return OGS_OK;
   return set_error(OGS_EDEVICE, std::string(fn) + ": " + what + ": " + cudaGetErrorString(e));
+}
+
+// Copy streams and events of the host-buffer pipeline, made on first use.
+ogs_status ensure_pipeline(ogs_handle_s* h, const char* fn) {
+  const size_t need = 1 + 2 * h->lay.phases.size();
+  if (h->copy_in && h->events.size() >= need) return OGS_OK;
+  ogs_status s;
+  if (!h->copy_in) {
+    cudaStream_t a = nullptr, b = nullptr;
+    if ((s = cuda_status(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking), fn, "stream")) != OGS_OK) return s;
+    if ((s = cuda_status(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking), fn, "stream")) != OGS_OK) {
+      cudaStreamDestroy(a);
+      return s;
+    }
+    h->copy_in = a;
+    h->copy_out = b;
+  }
+  while (h->events.size() < need) {
+    cudaEvent_t e = nullptr;
+    if ((s = cuda_status(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), fn, "event")) != OGS_OK) return s;
+    h->events.push_back(e);
+  }
+  return OGS_OK;
 }
 
 }  // namespace
@@ -231,17 +263,58 @@ ogs_status ogs_gather_scatter_host(ogs_handle h, void* v, int k, int type, int o
   if (s != OGS_OK) return s;
   if (h->N == 0) return OGS_OK;
   if (!v) return set_error(OGS_EINVAL, "ogs_gather_scatter_host: v is NULL");
-  const size_t bytes = static_cast<size_t>(h->N) * k * type_size(type);
+  const size_t node_bytes = static_cast<size_t>(k) * type_size(type);
+  const size_t bytes = static_cast<size_t>(h->N) * node_bytes;
   if ((s = ensure_stage(h, bytes, fn)) != OGS_OK) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if ((s = cuda_status(cudaMemcpyAsync(h->stage, v, bytes, cudaMemcpyHostToDevice, st), fn, "copy in")) != OGS_OK)
-    return s;
   FieldArgs f{};
   f.v = h->stage;
   f.K = k;
-  if ((s = launch(h, f, kModeGS, op, pattern_for(h, kModeGS, trans), type, stream, fn)) != OGS_OK) return s;
-  if ((s = cuda_status(cudaMemcpyAsync(v, h->stage, bytes, cudaMemcpyDeviceToHost, st), fn, "copy out")) != OGS_OK)
-    return s;
+  const Pattern pat = pattern_for(h, kModeGS, trans);
+  if (OGS_KERNEL != 0 || h->lay.phases.size() < 2) {
+    if ((s = cuda_status(cudaMemcpyAsync(h->stage, v, bytes, cudaMemcpyHostToDevice, st), fn, "copy in")) != OGS_OK)
+      return s;
+    if ((s = launch(h, f, kModeGS, op, pat, type, stream, fn)) != OGS_OK) return s;
+    if ((s = cuda_status(cudaMemcpyAsync(v, h->stage, bytes, cudaMemcpyDeviceToHost, st), fn, "copy out")) !=
+        OGS_OK)
+      return s;
+    return cuda_status(cudaStreamSynchronize(st), fn, "synchronize");
+  }
+  // Pipelined: chunk p goes in on copy_in while phase p-1 runs on `stream`
+  // and the nodes that phase p-2 finished go out on copy_out.
+  if ((s = ensure_pipeline(h, fn)) != OGS_OK) return s;
+  cudaStream_t sin = static_cast<cudaStream_t>(h->copy_in);
+  cudaStream_t sout = static_cast<cudaStream_t>(h->copy_out);
+  auto ev = [&](size_t i) { return static_cast<cudaEvent_t>(h->events[i]); };
+  char* dv = static_cast<char*>(h->stage);
+  char* hv = static_cast<char*>(v);
+  const std::vector<Phase>& ph = h->lay.phases;
+  const size_t P = ph.size();
+  // work already queued on the caller's stream comes first
+  if ((s = cuda_status(cudaEventRecord(ev(0), st), fn, "event")) != OGS_OK) return s;
+  if ((s = cuda_status(cudaStreamWaitEvent(sin, ev(0), 0), fn, "wait")) != OGS_OK) return s;
+  for (size_t p = 0; p < P; ++p) {
+    const size_t off = static_cast<size_t>(ph[p].h0) * node_bytes, len = static_cast<size_t>(ph[p].h1 - ph[p].h0) * node_bytes;
+    if (len && (s = cuda_status(cudaMemcpyAsync(dv + off, hv + off, len, cudaMemcpyHostToDevice, sin), fn,
+                                "copy in")) != OGS_OK)
+      return s;
+    if ((s = cuda_status(cudaEventRecord(ev(1 + 2 * p), sin), fn, "event")) != OGS_OK) return s;
+  }
+  for (size_t p = 0; p < P; ++p) {
+    if ((s = cuda_status(cudaStreamWaitEvent(st, ev(1 + 2 * p), 0), fn, "wait")) != OGS_OK) return s;
+    if ((s = launch_maps(phase_maps(h->dmaps, ph[p]), f, kModeGS, op, pat, type, stream, fn)) != OGS_OK) return s;
+    if ((s = cuda_status(cudaEventRecord(ev(2 + 2 * p), st), fn, "event")) != OGS_OK) return s;
+  }
+  for (size_t p = 0; p < P; ++p) {
+    const size_t off = static_cast<size_t>(ph[p].d0) * node_bytes, len = static_cast<size_t>(ph[p].d1 - ph[p].d0) * node_bytes;
+    if (!len) continue;
+    if ((s = cuda_status(cudaStreamWaitEvent(sout, ev(2 + 2 * p), 0), fn, "wait")) != OGS_OK) return s;
+    if ((s = cuda_status(cudaMemcpyAsync(hv + off, dv + off, len, cudaMemcpyDeviceToHost, sout), fn, "copy out")) !=
+        OGS_OK)
+      return s;
+  }
+  if ((s = cuda_status(cudaStreamSynchronize(sout), fn, "synchronize")) != OGS_OK) return s;
+  if ((s = cuda_status(cudaStreamSynchronize(sin), fn, "synchronize")) != OGS_OK) return s;
   return cuda_status(cudaStreamSynchronize(st), fn, "synchronize");
 }
 
@@ -342,11 +415,19 @@ ogs_status ogs_get_maps(ogs_handle h, int32_t* rowStartsT, int32_t* colIdsT, int
 ogs_status ogs_get_layout_stats(ogs_handle h, ogs_layout_stats* out) {
   if (!h || !out) return set_error(OGS_EINVAL, "ogs_get_layout_stats: NULL argument");
   std::memset(out, 0, sizeof(*out));
-  for (int d = 1; d <= kDmax; ++d) out->rows_by_degree[d] = static_cast<int64_t>(h->lay.rows[d].size());
+  for (int d = 1; d <= kDmax; ++d) out->rows_by_degree[d] = h->lay.n[d];
   out->rows_by_degree[0] = static_cast<int64_t>(h->lay.g_rows.size());
   out->nnz_general = static_cast<int64_t>(h->lay.g_colsT.size());
   out->ntiles = static_cast<int64_t>(h->lay.tiles.size());
   out->device_bytes = static_cast<int64_t>(h->arena_bytes);
+  out->nphases = static_cast<int64_t>(h->lay.phases.size());
+  for (size_t p = 0; p < h->lay.phases.size() && p < 8; ++p) {
+    const Phase& q = h->lay.phases[p];
+    out->phases[p][0] = q.lo;
+    out->phases[p][1] = q.hi;
+    out->phases[p][2] = q.h1;
+    out->phases[p][3] = q.d1;
+  }
   return OGS_OK;
 }
 

@@ -28,8 +28,22 @@ constexpr int kTileNnz = 2048;
 constexpr int kEntriesPerThread = kTileNnz / kBlock;
 // General-bucket tiles hold at most one row per thread.
 constexpr int kGeneralRowsPerTile = kBlock;
+// A warp tile prefetches, into L2, what the tile this many positions later
+// in the sweep will read (about two waves of resident warps ahead; 0 = off).
+#ifndef OGS_PREFETCH_AHEAD
+#define OGS_PREFETCH_AHEAD 8192
+#endif
+constexpr int kPrefetchAhead = OGS_PREFETCH_AHEAD;
 // Separate arrays handled by one launch of the *_many entry points.
 constexpr int kMaxMany = 16;
+// Member entries per lane of a warp tile (ogs_warp.cuh): lane l owns
+// kWarpEntries/d rows of degree d (at least one); the per-lane arrays hold up
+// to kWarpSlots entries.
+#ifndef OGS_WARP_ENTRIES
+#define OGS_WARP_ENTRIES 8
+#endif
+constexpr int kWarpEntries = OGS_WARP_ENTRIES;
+constexpr int kWarpSlots = kWarpEntries > kDmax ? kWarpEntries : kDmax;
 
 // Rows of degree d that one thread handles in a tile (at least one).
 OGS_HD inline constexpr int rows_per_thread(int d) {
@@ -38,14 +52,22 @@ OGS_HD inline constexpr int rows_per_thread(int d) {
 OGS_HD inline constexpr int rows_per_tile(int d) {
   return d >= 1 && d <= kDmax ? kBlock * rows_per_thread(d) : kGeneralRowsPerTile;
 }
+OGS_HD inline constexpr int warp_rows_per_lane(int d) {
+  return (kWarpEntries / d) > 0 ? (kWarpEntries / d) : 1;
+}
+OGS_HD inline constexpr int warp_rows_per_tile(int d) { return 32 * warp_rows_per_lane(d); }
 
 // One bucket of rows of exact degree d, rows in ascending row order.
+// Arrays are padded (stride = n rounded up to 4 rows, masks to 16 bytes) so
+// that every tile's chunk starts on a 16-byte boundary and may be copied with
+// its length rounded up, as the bulk (TMA) copies require.
 struct DevBucket {
-  const int32_t* cols;   // [d][n]: member j of bucket row i at cols[j*n + i]
-  const int32_t* rows;   // [n] row ids (ascending)
-  const uint8_t* nmask;  // [n] bit j set when member j is in the N map (Signed only)
+  const int32_t* cols;   // [d][stride]: member j of bucket row i at cols[j*stride + i]
+  const int32_t* rows;   // [stride] row ids (ascending)
+  const uint8_t* nmask;  // [stride rounded to 16] bit j: member j is in the N map (Signed only)
   int32_t n;             // rows in the bucket
   int32_t nP;            // rows with row id < NrowsN, a prefix of the bucket
+  int32_t stride;        // n rounded up to a multiple of 4
 };
 
 // Rows of degree > kDmax, CSR relative to the bucket.
@@ -68,12 +90,55 @@ struct Tile {
   int32_t first_row;
 };
 
+// One warp tile as a self-contained 32-byte record, for launches that walk
+// the tiles of several meshes (ogs_batch.cuh).
+struct WarpRec {
+  const int32_t* cols;     // the bucket's column ids (member q of row i at cols[q*stride + i])
+  const int32_t* rows;     // the bucket's row ids
+  const int32_t* pf_cols;  // column ids of the bucket of the tile prefetched for
+  int32_t begin;           // first bucket row of the tile
+  int32_t bucket_count;    // degree << 16 | rows in the tile
+  int32_t stride;          // the bucket's stride
+  int32_t nP;              // bucket rows below NrowsN
+  int32_t pf_lo, pf_hi;    // as WTile
+  int32_t pf_begin, pf_bucket_count;
+  int32_t pf_stride;
+  int32_t pad;
+};
+static_assert(sizeof(WarpRec) == 64, "WarpRec is 64 bytes");
+
+// One entry of a batched launch, in device memory.
+struct BatchEntry {
+  const WarpRec* recs;     // the handle's warp records
+  const uint8_t* wemask;   // the handle's per-lane N masks (Signed only)
+  void* v;                 // field, K interleaved components per node
+  int32_t K, op;
+  int32_t gather_n, scatter_n, limit_n, use_mask;
+};
+
+// A warp tile (ogs_warp.cuh) with the L2 prefetch it issues for the tile
+// kPrefetchAhead positions later: field nodes [pf_lo, pf_hi) that no earlier
+// tile has asked for, and the column-id chunks of that later tile.
+struct WTile {
+  int32_t bucket, begin, count, first_row;
+  int32_t pf_lo, pf_hi;      // node range, empty when pf_hi <= pf_lo
+  int32_t pf_begin;          // first bucket row of the later tile
+  int32_t pf_bucket_count;   // its degree << 16 | rows (0: none)
+};
+static_assert(sizeof(WTile) == 32, "WTile is 32 bytes");
+
 struct DevMaps {
   DevBucket b[kDmax + 1];  // b[0] unused
   DevGeneral g;
-  const Tile* tiles;
+  const Tile* tiles;       // CTA tiles of every bucket, ordered by first row (direct kernel)
   int32_t ntiles;
   int32_t signed_maps;     // N maps differ from T maps
+  int32_t ngtiles;         // general-bucket CTA tiles, ordered by first row
+  const Tile* gtiles;
+  const WTile* wtiles;     // exact-degree warp tiles (ogs_warp.cuh), ordered by first row
+  const uint8_t* wemask;   // [nwtiles][32] per-lane entry masks of the N map (Signed only)
+  int32_t nwtiles;
+  const WarpRec* wrecs;    // [nwtiles] the warp tiles as records (batched launches)
 };
 
 // Which members take part, per ogsOperator.cpp:60-97, 206-238, 311-360.
@@ -95,15 +160,30 @@ struct FieldArgs {
   int32_t is_many;
 };
 
+// A slice of the warp and general tiles for the host-buffer pipeline: its
+// kernels read and write local nodes in [lo, hi]; its host->device chunk is
+// [h0, h1) and once it has run, local nodes [d0, d1) are final and go back.
+struct Phase {
+  int32_t w0, w1;  // warp tiles
+  int32_t g0, g1;  // general tiles
+  int64_t lo, hi;
+  int64_t h0, h1, d0, d1;
+};
+
 // Host-side copy of everything built at setup.
 struct HostLayout {
   std::vector<int32_t> cols[kDmax + 1];
   std::vector<int32_t> rows[kDmax + 1];
   std::vector<uint8_t> nmask[kDmax + 1];
   int32_t nP[kDmax + 1] = {0};
+  int32_t n[kDmax + 1] = {0};
   std::vector<int32_t> g_rows, g_startsT, g_colsT, g_startsN, g_colsN;
   int32_t g_nP = 0;
-  std::vector<Tile> tiles;
+  std::vector<Tile> tiles;   // CTA tiles, all buckets, by first row
+  std::vector<Tile> gtiles;  // general CTA tiles, by first row
+  std::vector<WTile> wtiles; // exact-degree warp tiles, by first row
+  std::vector<uint8_t> wemask;
+  std::vector<Phase> phases;
 };
 
 }  // namespace ogsgb
@@ -129,6 +209,9 @@ struct ogs_handle_s {
 
   void* stage = nullptr;  // device staging for the _host entry points
   size_t stage_bytes = 0;
+  void* copy_in = nullptr;   // cudaStream_t: host->device chunks of the host pipeline
+  void* copy_out = nullptr;  // cudaStream_t: device->host chunks
+  std::vector<void*> events; // cudaEvent_t: [0] call start, then 2 per phase
 };
 
 namespace ogsgb {
@@ -138,12 +221,25 @@ ogs_status build_host_maps(ogs_handle_s* h, int64_t N, int64_t* ids, int kind, i
 void build_layout(ogs_handle_s* h);
 ogs_status upload_layout(ogs_handle_s* h);
 void release_device(ogs_handle_s* h);
+void build_phases(ogs_handle_s* h, int max_phases);
+void build_prefetch(HostLayout& L, int ahead);
+// DevMaps restricted to the tiles of one phase.
+DevMaps phase_maps(const DevMaps& m, const Phase& p);
 
-// Per-type launchers (ogs_kern_*.cu).  Return a cudaError_t value.
+// Per-type launchers (ogs_kern_*.cu).  Return a cudaError_t value.  k = 1
+// interleaved fields take the pipelined kernel over the exact-degree tiles
+// plus the direct kernel over the general tiles; every other case runs the
+// direct kernel over all tiles.
 int launch_f32(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, void* stream);
 int launch_f64(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, void* stream);
 int launch_i32(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, void* stream);
 int launch_i64(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, void* stream);
+
+// Batched launch over `n` entries (ogs_batch.cuh); grid <= 0 = one full wave.
+int launch_batch_f32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream);
+int launch_batch_f64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream);
+int launch_batch_i32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream);
+int launch_batch_i64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream);
 
 // Thread-local error message (ogs_capi.cpp).
 ogs_status set_error(ogs_status s, const std::string& msg);

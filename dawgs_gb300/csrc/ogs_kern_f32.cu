@@ -1,9 +1,13 @@
 // ogs_kern_f32.cu -- float instantiation of the tile kernels (one translation
 // unit per value type so the four compile in parallel).
-#include "ogs_kernels.cuh"
+#include "ogs_batch.cuh"
+#include "ogs_launch.cuh"
 
 namespace ogsgb {
 int launch_f32(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, void* stream) {
   return launch_typed<float>(m, f, mode, op, pat, stream);
+}
+int launch_batch_f32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream) {
+  return launch_batch_typed<float>(E, starts, n, nitems, grid, stream);
 }
 }  // namespace ogsgb

@@ -1,9 +1,13 @@
 // ogs_kern_i64.cu -- int64_t instantiation of the tile kernels (one translation
 // unit per value type so the four compile in parallel).
-#include "ogs_kernels.cuh"
+#include "ogs_batch.cuh"
+#include "ogs_launch.cuh"
 
 namespace ogsgb {
 int launch_i64(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, void* stream) {
   return launch_typed<int64_t>(m, f, mode, op, pat, stream);
+}
+int launch_batch_i64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream) {
+  return launch_batch_typed<int64_t>(E, starts, n, nitems, grid, stream);
 }
 }  // namespace ogsgb

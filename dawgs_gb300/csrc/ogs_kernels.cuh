@@ -78,7 +78,7 @@ __device__ __forceinline__ void run_fixed(const DevBucket& b, const Tile& t, con
   constexpr int RPT = rows_per_thread(D);
   int end = t.begin + t.count;
   if (pat.limit_n) end = min(end, b.nP);
-  const int n = b.n;
+  const int n = b.stride;
   const bool use_mask = (pat.gather_n || pat.scatter_n) && b.nmask != nullptr;
 
   int idx[RPT];
@@ -204,33 +204,13 @@ __global__ void __launch_bounds__(kBlock) ogs_tiles_kernel(const DevMaps m, cons
 }
 
 template <typename T, int OP, int MODE>
-inline cudaError_t launch_mode(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
+inline cudaError_t launch_direct(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
+  if (m.ntiles == 0) return cudaSuccess;
   const dim3 grid(static_cast<unsigned>(m.ntiles)), block(kBlock);
   if (f.K == 1 && !f.is_many) ogs_tiles_kernel<T, OP, MODE, true><<<grid, block, 0, s>>>(m, f, pat);
   else ogs_tiles_kernel<T, OP, MODE, false><<<grid, block, 0, s>>>(m, f, pat);
   return cudaGetLastError();
 }
 
-template <typename T, int MODE>
-inline cudaError_t launch_op(const DevMaps& m, const FieldArgs& f, int op, Pattern pat, cudaStream_t s) {
-  switch (op) {
-    case OGS_ADD: return launch_mode<T, OGS_ADD, MODE>(m, f, pat, s);
-    case OGS_MUL: return launch_mode<T, OGS_MUL, MODE>(m, f, pat, s);
-    case OGS_MAX: return launch_mode<T, OGS_MAX, MODE>(m, f, pat, s);
-    default: return launch_mode<T, OGS_MIN, MODE>(m, f, pat, s);
-  }
-}
-
-template <typename T>
-inline int launch_typed(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat,
-                        void* stream) {
-  if (m.ntiles == 0) return 0;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e;
-  if (mode == kModeGS) e = launch_op<T, kModeGS>(m, f, op, pat, s);
-  else if (mode == kModeGather) e = launch_op<T, kModeGather>(m, f, op, pat, s);
-  else e = launch_mode<T, OGS_ADD, kModeScatter>(m, f, pat, s);  // a copy: op unused
-  return static_cast<int>(e);
-}
-
 }  // namespace ogsgb
+

@@ -1,0 +1,44 @@
+// ogs_launch.cuh -- per-type launch dispatch shared by ogs_kern_*.cu.
+//
+// Exact-degree rows run on the warp-pipelined kernel (ogs_warp.cuh) for every
+// k and layout; rows above degree 8 on the direct CTA kernel
+// (ogs_kernels.cuh).  Building with -DOGS_KERNEL=2 runs the direct CTA
+// kernel for every row instead (for comparisons).
+#pragma once
+
+#include "ogs_warp.cuh"
+
+#ifndef OGS_KERNEL
+#define OGS_KERNEL 0
+#endif
+
+namespace ogsgb {
+
+template <typename T, int OP, int MODE>
+inline cudaError_t launch_mode(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
+  if (OGS_KERNEL == 2) return launch_direct<T, OP, MODE>(m, f, pat, s);
+  return launch_warp<T, OP, MODE>(m, f, pat, s);
+}
+
+template <typename T, int MODE>
+inline cudaError_t launch_op(const DevMaps& m, const FieldArgs& f, int op, Pattern pat, cudaStream_t s) {
+  switch (op) {
+    case OGS_ADD: return launch_mode<T, OGS_ADD, MODE>(m, f, pat, s);
+    case OGS_MUL: return launch_mode<T, OGS_MUL, MODE>(m, f, pat, s);
+    case OGS_MAX: return launch_mode<T, OGS_MAX, MODE>(m, f, pat, s);
+    default: return launch_mode<T, OGS_MIN, MODE>(m, f, pat, s);
+  }
+}
+
+template <typename T>
+inline int launch_typed(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, void* stream) {
+  if (m.ntiles == 0) return 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (mode == kModeGS) e = launch_op<T, kModeGS>(m, f, op, pat, s);
+  else if (mode == kModeGather) e = launch_op<T, kModeGather>(m, f, op, pat, s);
+  else e = launch_mode<T, OGS_ADD, kModeScatter>(m, f, pat, s);  // a copy: op unused
+  return static_cast<int>(e);
+}
+
+}  // namespace ogsgb

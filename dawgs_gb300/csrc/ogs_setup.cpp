@@ -20,6 +20,7 @@
 #include <chrono>
 #include <cstdio>
 #include <cstring>
+#include <climits>
 #include <limits>
 
 #include <cuda_runtime.h>
@@ -194,11 +195,14 @@ void build_layout(ogs_handle_s* h) {
     if (d <= kDmax) cnt[d]++;
     else { cnt[0]++; gnnzT += d; gnnzN += rsN[r + 1] - rsN[r]; }
   }
+  int64_t stride[kDmax + 1] = {0};
   for (int d = 1; d <= kDmax; ++d) {
-    L.cols[d].assign(static_cast<size_t>(cnt[d]) * d, 0);
-    L.rows[d].assign(cnt[d], 0);
-    L.nmask[d].assign(sgn ? cnt[d] : 0, 0);
+    stride[d] = (cnt[d] + 3) / 4 * 4;
+    L.cols[d].assign(static_cast<size_t>(stride[d]) * d, 0);
+    L.rows[d].assign(stride[d], 0);
+    L.nmask[d].assign(sgn ? (cnt[d] + 15) / 16 * 16 : 0, 0);
     L.nP[d] = 0;
+    L.n[d] = static_cast<int32_t>(cnt[d]);
   }
   L.g_rows.clear(); L.g_startsT.assign(1, 0); L.g_colsT.clear();
   L.g_startsN.assign(1, 0); L.g_colsN.clear();
@@ -211,7 +215,7 @@ void build_layout(ogs_handle_s* h) {
     const bool inP = r < h->NlocalP;
     if (d <= kDmax) {
       const int64_t i = fill[d]++;
-      const int64_t n = cnt[d];
+      const int64_t n = stride[d];
       L.rows[d][i] = static_cast<int32_t>(r);
       if (inP) L.nP[d]++;
       uint8_t mask = 0;
@@ -236,6 +240,7 @@ void build_layout(ogs_handle_s* h) {
   // Tiles: fixed row counts per exact-degree bucket, greedy packing of the
   // general bucket; then ordered by first row id.
   L.tiles.clear();
+  L.gtiles.clear();
   for (int d = 1; d <= kDmax; ++d) {
     const int32_t n = static_cast<int32_t>(cnt[d]);
     const int32_t step = rows_per_tile(d);
@@ -253,15 +258,162 @@ void build_layout(ogs_handle_s* h) {
         nnz += dj;
         j++;
       }
-      L.tiles.push_back(Tile{0, i, j - i, L.g_rows[i]});
+      L.gtiles.push_back(Tile{0, i, j - i, L.g_rows[i]});
       i = j;
     }
   }
-  std::stable_sort(L.tiles.begin(), L.tiles.end(),
-                   [](const Tile& a, const Tile& b) { return a.first_row < b.first_row; });
+  auto by_row = [](const Tile& a, const Tile& b) { return a.first_row < b.first_row; };
+  // warp tiles and, for Signed maps, each lane's entry mask: bit j*d+q set
+  // when member q of the lane's row j is in the N map
+  L.wtiles.clear();
+  for (int d = 1; d <= kDmax; ++d) {
+    const int32_t n = static_cast<int32_t>(cnt[d]);
+    const int32_t step = warp_rows_per_tile(d);
+    for (int32_t i = 0; i < n; i += step)
+      L.wtiles.push_back(WTile{d, i, std::min(step, n - i), L.rows[d][i], 0, 0, 0, 0});
+  }
+  std::stable_sort(L.wtiles.begin(), L.wtiles.end(),
+                   [](const WTile& a, const WTile& b) { return a.first_row < b.first_row; });
+  L.wemask.assign(sgn ? L.wtiles.size() * 32 : 0, 0);
+  if (sgn) {
+    for (size_t t = 0; t < L.wtiles.size(); ++t) {
+      const WTile& w = L.wtiles[t];
+      const int d = w.bucket;
+      for (int lane = 0; lane < 32; ++lane) {
+        uint32_t bits = 0;
+        for (int j = 0; j < warp_rows_per_lane(d); ++j) {
+          const int r = j * 32 + lane;
+          if (r >= w.count) continue;
+          const uint32_t mk = L.nmask[d][w.begin + r];
+          for (int q = 0; q < d; ++q) bits |= ((mk >> q) & 1u) << (j * d + q);
+        }
+        L.wemask[t * 32 + lane] = static_cast<uint8_t>(bits);
+      }
+    }
+  }
+  L.tiles.insert(L.tiles.end(), L.gtiles.begin(), L.gtiles.end());
+  std::stable_sort(L.tiles.begin(), L.tiles.end(), by_row);
+  build_prefetch(L, kPrefetchAhead);
+  build_phases(h, 8);
+}
+
+// Tile t asks L2 for what tile t+ahead will read: the field nodes above the
+// highest node any tile before it reaches, and its column-id chunks.  Tiles
+// are in row (first appearance) order, so the highest node reached grows
+// with t and every node is asked for once.
+void build_prefetch(HostLayout& L, int ahead) {
+  const int64_t nw = static_cast<int64_t>(L.wtiles.size());
+  std::vector<int32_t> cummax(nw);
+  int32_t run = -1;
+  for (int64_t t = 0; t < nw; ++t) {
+    const WTile& w = L.wtiles[t];
+    const int d = w.bucket;
+    const int64_t stride = static_cast<int64_t>(L.rows[d].size());
+    for (int q = 0; q < d; ++q)
+      for (int32_t r = 0; r < w.count; ++r) run = std::max(run, L.cols[d][q * stride + w.begin + r]);
+    cummax[t] = run;
+  }
+  for (int64_t t = 0; t < nw; ++t) {
+    WTile& w = L.wtiles[t];
+    const int64_t u = t + ahead;
+    if (ahead <= 0 || u >= nw) {
+      w.pf_lo = w.pf_hi = w.pf_begin = w.pf_bucket_count = 0;
+      continue;
+    }
+    w.pf_lo = cummax[u - 1] + 1;
+    w.pf_hi = cummax[u] + 1;
+    w.pf_begin = L.wtiles[u].begin;
+    w.pf_bucket_count = (L.wtiles[u].bucket << 16) | L.wtiles[u].count;
+  }
+}
+
+void build_phases(ogs_handle_s* h, int max_phases) {
+  HostLayout& L = h->lay;
+  L.phases.clear();
+  const int32_t nw = static_cast<int32_t>(L.wtiles.size());
+  const int32_t ng = static_cast<int32_t>(L.gtiles.size());
+  if (nw + ng == 0) return;
+  int P = nw / 256;
+  if (P < 1) P = 1;
+  if (P > max_phases) P = max_phases;
+  // phase boundaries in warp tiles; general tiles follow by first row
+  for (int p = 0; p < P; ++p) {
+    Phase ph{};
+    ph.w0 = static_cast<int32_t>(static_cast<int64_t>(nw) * p / P);
+    ph.w1 = static_cast<int32_t>(static_cast<int64_t>(nw) * (p + 1) / P);
+    L.phases.push_back(ph);
+  }
+  int32_t g = 0;
+  for (int p = 0; p < P; ++p) {
+    Phase& ph = L.phases[p];
+    ph.g0 = g;
+    const bool last = (p == P - 1);
+    const int32_t row_end = last || ph.w1 >= nw ? INT32_MAX : L.wtiles[ph.w1].first_row;
+    while (g < ng && (last || L.gtiles[g].first_row < row_end)) g++;
+    ph.g1 = g;
+    int64_t lo = INT64_MAX, hi = -1;
+    for (int32_t t = ph.w0; t < ph.w1; ++t) {
+      const WTile& w = L.wtiles[t];
+      const int d = w.bucket;
+      const int64_t stride = static_cast<int64_t>(L.rows[d].size());
+      for (int q = 0; q < d; ++q)
+        for (int32_t r = 0; r < w.count; ++r) {
+          const int64_t c = L.cols[d][q * stride + w.begin + r];
+          lo = std::min(lo, c);
+          hi = std::max(hi, c);
+        }
+    }
+    for (int32_t t = ph.g0; t < ph.g1; ++t) {
+      const Tile& w = L.gtiles[t];
+      for (int32_t q = L.g_startsT[w.begin]; q < L.g_startsT[w.begin + w.count]; ++q) {
+        lo = std::min<int64_t>(lo, L.g_colsT[q]);
+        hi = std::max<int64_t>(hi, L.g_colsT[q]);
+      }
+    }
+    ph.lo = lo;
+    ph.hi = hi;
+  }
+  // host->device chunk p: up to the highest node phases <= p touch (all of N at the end)
+  int64_t need = 0;
+  for (int p = 0; p < P; ++p) {
+    Phase& ph = L.phases[p];
+    ph.h0 = need;
+    need = std::max(need, ph.hi + 1);
+    if (p == P - 1) need = h->N;
+    ph.h1 = need;
+  }
+  // device->host chunk p: nodes below the lowest node any later phase touches
+  int64_t fin = h->N;
+  std::vector<int64_t> final_at(P);
+  for (int p = P - 1; p >= 0; --p) {
+    final_at[p] = fin;
+    fin = std::min(fin, L.phases[p].lo);
+  }
+  int64_t prev = 0;
+  for (int p = 0; p < P; ++p) {
+    L.phases[p].d0 = prev;
+    L.phases[p].d1 = std::max(prev, final_at[p]);
+    prev = L.phases[p].d1;
+  }
+}
+
+DevMaps phase_maps(const DevMaps& m, const Phase& p) {
+  DevMaps r = m;
+  r.wtiles = m.wtiles + p.w0;
+  r.nwtiles = p.w1 - p.w0;
+  if (m.wemask) r.wemask = m.wemask + static_cast<int64_t>(p.w0) * 32;
+  r.gtiles = m.gtiles + p.g0;
+  r.ngtiles = p.g1 - p.g0;
+  r.ntiles = r.nwtiles + r.ngtiles;
+  return r;
 }
 
 void release_device(ogs_handle_s* h) {
+  for (void* e : h->events) cudaEventDestroy(static_cast<cudaEvent_t>(e));
+  h->events.clear();
+  if (h->copy_in) cudaStreamDestroy(static_cast<cudaStream_t>(h->copy_in));
+  if (h->copy_out) cudaStreamDestroy(static_cast<cudaStream_t>(h->copy_out));
+  h->copy_in = h->copy_out = nullptr;
   if (h->arena) cudaFree(h->arena);
   if (h->stage) cudaFree(h->stage);
   h->arena = nullptr;
@@ -294,6 +446,12 @@ ogs_status upload_layout(ogs_handle_s* h) {
   const size_t o_gsN = sgn ? add(L.g_startsN.data(), L.g_startsN.size() * 4) : o_gsT;
   const size_t o_gcN = sgn ? add(L.g_colsN.data(), L.g_colsN.size() * 4) : o_gcT;
   const size_t o_tiles = add(L.tiles.data(), L.tiles.size() * sizeof(Tile));
+  const size_t o_gtiles = add(L.gtiles.data(), L.gtiles.size() * sizeof(Tile));
+  const size_t o_wtiles = add(L.wtiles.data(), L.wtiles.size() * sizeof(WTile));
+  const size_t o_wemask = add(L.wemask.data(), L.wemask.size());
+  // warp records hold device pointers: filled in once the arena exists
+  std::vector<WarpRec> wrecs(L.wtiles.size());
+  const size_t o_wrecs = add(wrecs.data(), wrecs.size() * sizeof(WarpRec));
 
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -304,6 +462,24 @@ ogs_status upload_layout(ogs_handle_s* h) {
     cudaGetLastError();
     return set_error(e == cudaErrorMemoryAllocation ? OGS_ENOMEM : OGS_EDEVICE,
                      std::string("cudaMalloc of maps: ") + cudaGetErrorString(e));
+  }
+  for (size_t t = 0; t < L.wtiles.size(); ++t) {
+    const WTile& w = L.wtiles[t];
+    WarpRec& r = wrecs[t];
+    r.cols = reinterpret_cast<const int32_t*>(base + o_cols[w.bucket]);
+    r.rows = reinterpret_cast<const int32_t*>(base + o_rows[w.bucket]);
+    r.begin = w.begin;
+    r.bucket_count = (w.bucket << 16) | w.count;
+    r.stride = static_cast<int32_t>(L.rows[w.bucket].size());
+    r.nP = L.nP[w.bucket];
+    r.pf_lo = w.pf_lo;
+    r.pf_hi = w.pf_hi;
+    r.pf_begin = w.pf_begin;
+    r.pf_bucket_count = w.pf_bucket_count;
+    const int pd = w.pf_bucket_count >> 16;
+    r.pf_cols = pd ? reinterpret_cast<const int32_t*>(base + o_cols[pd]) : nullptr;
+    r.pf_stride = pd ? static_cast<int32_t>(L.rows[pd].size()) : 0;
+    r.pad = 0;
   }
   for (const Piece& p : pieces) {
     if (!p.bytes) continue;
@@ -322,8 +498,9 @@ ogs_status upload_layout(ogs_handle_s* h) {
     m.b[d].cols = reinterpret_cast<const int32_t*>(base + o_cols[d]);
     m.b[d].rows = reinterpret_cast<const int32_t*>(base + o_rows[d]);
     m.b[d].nmask = sgn ? reinterpret_cast<const uint8_t*>(base + o_mask[d]) : nullptr;
-    m.b[d].n = static_cast<int32_t>(L.rows[d].size());
+    m.b[d].n = L.n[d];
     m.b[d].nP = L.nP[d];
+    m.b[d].stride = static_cast<int32_t>(L.rows[d].size());
   }
   m.g.rows = reinterpret_cast<const int32_t*>(base + o_grows);
   m.g.startsT = reinterpret_cast<const int32_t*>(base + o_gsT);
@@ -334,6 +511,13 @@ ogs_status upload_layout(ogs_handle_s* h) {
   m.g.nP = L.g_nP;
   m.tiles = reinterpret_cast<const Tile*>(base + o_tiles);
   m.ntiles = static_cast<int32_t>(L.tiles.size());
+  m.gtiles = reinterpret_cast<const Tile*>(base + o_gtiles);
+  m.ngtiles = static_cast<int32_t>(L.gtiles.size());
+  m.wtiles = reinterpret_cast<const WTile*>(base + o_wtiles);
+  m.nwtiles = static_cast<int32_t>(L.wtiles.size());
+  m.wemask = reinterpret_cast<const uint8_t*>(base + o_wemask);
+  m.wrecs = reinterpret_cast<const WarpRec*>(base + o_wrecs);
+
   m.signed_maps = sgn ? 1 : 0;
   return OGS_OK;
 }

@@ -1,0 +1,264 @@
+// ogs_warp.cuh -- persistent, warp-pipelined gather-scatter kernel.
+//
+// Arithmetic as in ogs_kernels.cuh (one fold per row from the op identity
+// over the members in ascending local index: ogsOperator.cpp:60-97, 206-238,
+// 311-360).  The data movement is organised per warp, with no block-level
+// synchronisation at all:
+//
+//  * Work items are (warp tile, component k).  A warp tile holds 32 lanes x
+//    kWarpEntries member entries of one exact-degree bucket: lane l owns rows
+//    l, l+32, ... of the tile, each with its d members.  Tiles are ordered by
+//    first row; warp w of the grid takes items w, w+W, w+2W, ... so the grid
+//    sweeps the mesh front to back and the nodes that neighbouring tiles share
+//    are served from L2.
+//  * Every iteration issues, back to back and without waiting: the value
+//    gathers of the current item, the column ids (and row ids / N masks) of
+//    the next item, and the descriptor of the item after that.  Only then does
+//    it fold the current rows and store the results.  One memory round trip
+//    per item instead of three (descriptor -> column ids -> values).
+//
+// Stores to the field never alias a later item's loads (every local node
+// belongs to one row), so loads and stores of different items may be in
+// flight together.
+#pragma once
+
+#include <cstdint>
+
+#include "ogs_kernels.cuh"
+
+// Minimum resident CTAs per SM the register allocation must allow.
+#ifndef OGS_WARP_MINB
+#define OGS_WARP_MINB 3
+#endif
+
+namespace ogsgb {
+
+// Column ids, row ids and the per-lane entry mask of one warp tile.
+struct WarpState {
+  int32_t I[kWarpSlots];  // entry e = j*D + q: member q of the lane's row j
+  int32_t R[kWarpSlots];  // row ids (Gather / Scatter only)
+  uint32_t emask;           // bit e: entry e is in the N map (Signed only)
+  int32_t cnt;              // rows of the tile this call processes
+};
+
+template <int MODE, int D, typename TileT>
+__device__ __forceinline__ void warp_load_state(const DevBucket& b, const TileT& t, const uint8_t* wemask,
+                                                int tile_index, bool use_mask, const Pattern& pat, int lane,
+                                                WarpState& s) {
+  constexpr int RPT = warp_rows_per_lane(D);
+  s.cnt = pat.limit_n ? min(t.count, b.nP - t.begin) : t.count;
+  s.emask = use_mask ? __ldg(wemask + static_cast<int64_t>(tile_index) * 32 + lane) : 0xFFu;
+#pragma unroll
+  for (int j = 0; j < RPT; ++j) {
+    const int r = j * 32 + lane;
+    if (r < s.cnt) {
+      const int idx = t.begin + r;
+#pragma unroll
+      for (int q = 0; q < D; ++q) s.I[j * D + q] = __ldg(b.cols + static_cast<int64_t>(q) * b.stride + idx);
+      if (MODE != kModeGS) s.R[j] = __ldg(b.rows + idx);
+    }
+  }
+}
+
+template <typename T, int MODE, int D>
+__device__ __forceinline__ void warp_load_vals(const WarpState& s, const T* src, const T* gv, int64_t stride,
+                                               int K, int k, bool gmask, int lane, T (&V)[kWarpSlots]) {
+  constexpr int RPT = warp_rows_per_lane(D);
+#pragma unroll
+  for (int j = 0; j < RPT; ++j) {
+    if (j * 32 + lane < s.cnt) {
+      if (MODE == kModeScatter) {
+        V[j] = gv[static_cast<int64_t>(s.R[j]) * K + k];
+      } else {
+#pragma unroll
+        for (int q = 0; q < D; ++q)
+          if (!gmask || ((s.emask >> (j * D + q)) & 1u)) V[j * D + q] = src[static_cast<int64_t>(s.I[j * D + q]) * stride];
+      }
+    }
+  }
+}
+
+template <typename T, int OP, int MODE, int D>
+__device__ __forceinline__ void warp_fold_store(const WarpState& s, T* dst, T* gv, int64_t stride, int K, int k,
+                                                bool gmask, bool smask, int lane, const T (&V)[kWarpSlots]) {
+  constexpr int RPT = warp_rows_per_lane(D);
+#pragma unroll
+  for (int j = 0; j < RPT; ++j) {
+    if (j * 32 + lane < s.cnt) {
+      T a;
+      if (MODE == kModeScatter) {
+        a = V[j];
+      } else {
+        a = op_init<T, OP>();
+#pragma unroll
+        for (int q = 0; q < D; ++q)
+          if (!gmask || ((s.emask >> (j * D + q)) & 1u)) op_apply<T, OP>(a, V[j * D + q]);
+      }
+      if (MODE == kModeGather) {
+        gv[static_cast<int64_t>(s.R[j]) * K + k] = a;
+      } else {
+#pragma unroll
+        for (int q = 0; q < D; ++q)
+          if (!smask || ((s.emask >> (j * D + q)) & 1u)) dst[static_cast<int64_t>(s.I[j * D + q]) * stride] = a;
+      }
+    }
+  }
+}
+
+// Asynchronous bulk prefetch of global bytes [a, b) into L2 (the TMA unit's
+// prefetch; no completion to wait for).  The range is shrunk to 16-byte
+// boundaries, as the instruction requires, so it never leaves the buffer.
+__device__ __forceinline__ void l2_prefetch(const void* a, const void* b) {
+  uintptr_t lo = (reinterpret_cast<uintptr_t>(a) + 15) & ~uintptr_t(15);
+  const uintptr_t hi = reinterpret_cast<uintptr_t>(b) & ~uintptr_t(15);
+  while (lo < hi) {
+    const uint32_t n = static_cast<uint32_t>(hi - lo < 65536 ? hi - lo : 65536);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"(n) : "memory");
+    lo += n;
+  }
+}
+
+// What a tile prefetches for the tile kPrefetchAhead positions later: the
+// field nodes [pf_lo, pf_hi) of every component array and that tile's
+// column-id chunks.
+template <typename T>
+__device__ __forceinline__ void prefetch_ahead(const FieldArgs& f, int K, int32_t pf_lo, int32_t pf_hi,
+                                               const int32_t* pf_cols, int32_t pf_stride, int32_t pf_begin,
+                                               int32_t pf_bucket_count) {
+  if (pf_hi > pf_lo) {
+    if (f.is_many) {
+      for (int k = 0; k < K; ++k) {
+        const T* a = static_cast<const T*>(f.many[k]);
+        l2_prefetch(a + pf_lo, a + pf_hi);
+      }
+    } else {
+      const T* a = static_cast<const T*>(f.v);
+      l2_prefetch(a + static_cast<int64_t>(pf_lo) * K, a + static_cast<int64_t>(pf_hi) * K);
+    }
+  }
+  const int pd = pf_bucket_count >> 16, pc = pf_bucket_count & 0xFFFF;
+  if (pd && pf_cols) {
+    const int32_t n4 = (pc + 3) & ~3;
+    for (int q = 0; q < pd; ++q) {
+      const int32_t* c = pf_cols + static_cast<int64_t>(q) * pf_stride + pf_begin;
+      l2_prefetch(c, c + n4);
+    }
+  }
+}
+
+#define OGS_DEGREE_SWITCH(bucket, CALL) \
+  switch (bucket) {                     \
+    case 1: CALL(1); break;             \
+    case 2: CALL(2); break;             \
+    case 3: CALL(3); break;             \
+    case 4: CALL(4); break;             \
+    case 5: CALL(5); break;             \
+    case 6: CALL(6); break;             \
+    case 7: CALL(7); break;             \
+    default: CALL(8); break;            \
+  }
+
+template <typename T, int OP, int MODE, bool K1>
+__global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const DevMaps m, const FieldArgs f,
+                                                                         const Pattern pat) {
+  const int lane = static_cast<int>(threadIdx.x) & 31;
+  const int64_t W = static_cast<int64_t>(gridDim.x) * (kBlock / 32);
+  const int K = K1 ? 1 : f.K;
+  const int64_t nitems = static_cast<int64_t>(m.nwtiles) * K;
+  int64_t i = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + (threadIdx.x >> 5);
+  if (i >= nitems) return;
+  const bool use_mask = (pat.gather_n || pat.scatter_n) && m.signed_maps;
+  const bool gmask = pat.gather_n != 0, smask = pat.scatter_n != 0;
+  const int64_t stride = K1 ? 1 : (f.is_many ? 1 : K);
+
+  int tcur = static_cast<int>(i / K);
+  WTile cur = m.wtiles[tcur];
+  WarpState scur;
+#define OGS_LOAD_CUR(D) warp_load_state<MODE, D>(m.b[D], cur, m.wemask, tcur, use_mask, pat, lane, scur)
+  OGS_DEGREE_SWITCH(cur.bucket, OGS_LOAD_CUR)
+#undef OGS_LOAD_CUR
+  WTile nxt{};
+  if (i + W < nitems) nxt = m.wtiles[(i + W) / K];
+
+  for (;;) {
+    const int k = K1 ? 0 : static_cast<int>(i % K);
+    if (lane == 0 && k == 0 && MODE != kModeScatter) {
+      const int pd = cur.pf_bucket_count >> 16;
+      const int32_t* pcols = nullptr;
+      int32_t pstride = 0;
+#define OGS_PF_COLS(D) pcols = m.b[D].cols; pstride = m.b[D].stride
+      if (pd) { OGS_DEGREE_SWITCH(pd, OGS_PF_COLS) }
+#undef OGS_PF_COLS
+      prefetch_ahead<T>(f, K, cur.pf_lo, cur.pf_hi, pcols, pstride, cur.pf_begin, cur.pf_bucket_count);
+    }
+    const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, k);
+    T* dst = (MODE == kModeGather) ? nullptr : field_base<T>(f, k);
+    T* gv = static_cast<T*>(f.gv);
+    T V[kWarpSlots];
+#define OGS_VALS(D) warp_load_vals<T, MODE, D>(scur, src, gv, stride, K, k, gmask, lane, V)
+    OGS_DEGREE_SWITCH(cur.bucket, OGS_VALS)
+#undef OGS_VALS
+    const bool more = i + W < nitems;
+    WarpState snxt;
+    WTile nn{};
+    int tnxt = 0;
+    if (more) {
+      tnxt = static_cast<int>((i + W) / K);
+#define OGS_LOAD_NXT(D) warp_load_state<MODE, D>(m.b[D], nxt, m.wemask, tnxt, use_mask, pat, lane, snxt)
+      OGS_DEGREE_SWITCH(nxt.bucket, OGS_LOAD_NXT)
+#undef OGS_LOAD_NXT
+      if (i + 2 * W < nitems) nn = m.wtiles[(i + 2 * W) / K];
+    }
+#define OGS_FOLD(D) warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, k, gmask, smask, lane, V)
+    OGS_DEGREE_SWITCH(cur.bucket, OGS_FOLD)
+#undef OGS_FOLD
+    if (!more) break;
+    i += W;
+    cur = nxt;
+    scur = snxt;
+    nxt = nn;
+    tcur = tnxt;
+  }
+}
+
+// CTAs of the warp kernel resident per SM, once per instantiation and device.
+template <typename T, int OP, int MODE, bool K1>
+inline int warp_grid(int64_t nitems) {
+  static int cached_dev = -1, cached = 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != cached_dev) {
+    int bps = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_warp_kernel<T, OP, MODE, K1>, kBlock, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cached = (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1);
+    cached_dev = dev;
+  }
+  const int64_t need = (nitems + (kBlock / 32) - 1) / (kBlock / 32);
+  return static_cast<int>(need < cached ? need : cached);
+}
+
+template <typename T, int OP, int MODE>
+inline cudaError_t launch_warp(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
+  const int64_t nitems = static_cast<int64_t>(m.nwtiles) * f.K;
+  if (nitems > 0) {
+    if (f.K == 1 && !f.is_many) {
+      const int grid = warp_grid<T, OP, MODE, true>(nitems);
+      ogs_warp_kernel<T, OP, MODE, true><<<grid, kBlock, 0, s>>>(m, f, pat);
+    } else {
+      const int grid = warp_grid<T, OP, MODE, false>(nitems);
+      ogs_warp_kernel<T, OP, MODE, false><<<grid, kBlock, 0, s>>>(m, f, pat);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (m.ngtiles > 0) {
+    DevMaps g = m;
+    g.tiles = m.gtiles;
+    g.ntiles = m.ngtiles;
+    return launch_direct<T, OP, MODE>(g, f, pat, s);
+  }
+  return cudaSuccess;
+}
+
+}  // namespace ogsgb

@@ -227,4 +227,59 @@ class ogs_t:
         check(lib().ogs_get_layout_stats(self.handle, C.byref(s)))
         return {"rows_by_degree": {d: int(s.rows_by_degree[d]) for d in range(1, 9) if s.rows_by_degree[d]},
                 "rows_general": int(s.rows_by_degree[0]), "nnz_general": int(s.nnz_general),
-                "ntiles": int(s.ntiles), "device_bytes": int(s.device_bytes)}
+                "ntiles": int(s.ntiles), "device_bytes": int(s.device_bytes),
+                "phases": [tuple(int(x) for x in s.phases[p]) for p in range(int(s.nphases))]}
+
+
+class ogs_batch_t:
+    """Many meshes' GatherScatters in one persistent launch (no reference
+    counterpart: dawgs calls ogs_t::GatherScatter once per mesh).
+
+    entries: list of (ogs_t, device field tensor, k, op, trans); all fields
+    share one dtype.  graph=True captures the launch in a CUDA graph on first
+    use and replays it afterwards."""
+
+    def __init__(self, entries, graph=False):
+        self._b = None
+        if not entries:
+            raise OgsError(_lib.OGS_EINVAL, "a batch needs at least one entry")
+        t = _type_of(entries[0][1])
+        arr = (_lib.OgsBatchEntry * len(entries))()
+        for i, (g, field, k, op, trans) in enumerate(entries):
+            if _type_of(field) != t:
+                raise OgsError(_lib.OGS_EINVAL, "all batch fields must share one dtype")
+            arr[i] = _lib.OgsBatchEntry(g.handle, _ptr(field), int(k), int(op), int(trans), 0)
+        b = C.c_void_p()
+        check(lib().ogs_batch_create(C.byref(b), int(t), arr, len(entries),
+                                     _lib.BATCH_GRAPH if graph else 0))
+        self._b = b
+        self.entries = entries
+
+    def GatherScatter(self, stream=None):
+        check(lib().ogs_batch_gather_scatter(self._b, _stream_of(stream)))
+
+    def set_fields(self, fields, stream=None):
+        arr = (C.c_void_p * len(fields))(*[_ptr(x) for x in fields])
+        check(lib().ogs_batch_set_fields(self._b, arr, _stream_of(stream)))
+
+    def tune(self, stream=None) -> int:
+        g = C.c_int()
+        check(lib().ogs_batch_tune(self._b, _stream_of(stream), C.byref(g)))
+        return g.value
+
+    @property
+    def items(self) -> int:
+        n = C.c_int64()
+        check(lib().ogs_batch_items(self._b, C.byref(n)))
+        return n.value
+
+    def Free(self):
+        if self._b is not None and _lib._lib is not None:
+            lib().ogs_batch_free(self._b)
+        self._b = None
+
+    def __del__(self):
+        try:
+            self.Free()
+        except Exception:
+            pass

@@ -36,7 +36,7 @@ typedef enum {
   OGS_EINVAL = 1,    /* bad argument or option set */
   OGS_ENOMEM = 2,    /* host or device allocation failed */
   OGS_EDEVICE = 3,   /* CUDA runtime error (message in ogs_last_error_string) */
-  OGS_ETIMEOUT = 4,  /* a bounded device-side wait ran out */
+  OGS_ETIMEOUT = 4,  /* reserved */
   OGS_ERANGE = 5,    /* sizes beyond 32-bit device indices or a stated limit */
   OGS_EUNDEFINED = 6 /* Gather/Scatter on a handle whose gather is not well-defined */
 } ogs_status;
@@ -73,6 +73,9 @@ typedef struct {
   int64_t nnz_general;       /* entries in rows above degree 8 */
   int64_t ntiles;            /* work tiles in one launch over the whole map */
   int64_t device_bytes;      /* device memory held by the handle's maps */
+  int64_t nphases;           /* slices of the host-buffer pipeline (at most 8) */
+  int64_t phases[8][4];      /* per slice: lowest and highest node it touches, end of its
+                                host->device chunk, end of the nodes final after it */
 } ogs_layout_stats;
 
 /* ogs_t::Setup (include/ogs.hpp:221-228; libs/ogs/ogsSetup.cpp:69-190).
@@ -129,6 +132,35 @@ ogs_status ogs_get_maps(ogs_handle h, int32_t *rowStartsT, int32_t *colIdsT,
                         int32_t *rowStartsN, int32_t *colIdsN);
 /* Degree buckets and tiles the kernels run over (no reference counterpart). */
 ogs_status ogs_get_layout_stats(ogs_handle h, ogs_layout_stats *out);
+
+/* ---- Batched gather-scatter: many meshes in one persistent launch ----
+ * No reference counterpart (dawgs calls ogs_t::GatherScatter once per mesh,
+ * dawgsMain.cpp:211-219).  Each entry applies the reference GatherScatter
+ * semantics (ogsOperator.cpp:311-360) with its own op, transpose and k to its
+ * own interleaved device field; the results equal one ogs_gather_scatter per
+ * entry bit for bit.  All entries share one value type and device.  Entries
+ * must not share a field buffer. */
+typedef struct ogs_batch_s *ogs_batch;
+typedef struct {
+  ogs_handle h;   /* mesh */
+  void *d_v;      /* device field: k interleaved components per node */
+  int32_t k;
+  int32_t op;     /* ogs_op */
+  int32_t trans;  /* ogs_transpose */
+  int32_t reserved;
+} ogs_batch_entry;
+#define OGS_BATCH_GRAPH 1u  /* capture the launch in a CUDA graph on first use, replay after */
+ogs_status ogs_batch_create(ogs_batch *out, int type, const ogs_batch_entry *entries, int n, unsigned flags);
+/* Point the entries at new fields (one per entry); synchronises `stream`. */
+ogs_status ogs_batch_set_fields(ogs_batch b, void *const *d_vs, void *stream);
+/* All entries' gather-scatters, asynchronously on `stream`. */
+ogs_status ogs_batch_gather_scatter(ogs_batch b, void *stream);
+/* Time the candidate launch shapes (1..6 persistent CTAs per SM) on the
+ * batch's own fields -- which they update in place -- and keep the fastest. */
+ogs_status ogs_batch_tune(ogs_batch b, void *stream, int *chosen_grid);
+/* Warp tiles the batched launch walks. */
+ogs_status ogs_batch_items(ogs_batch b, int64_t *items);
+ogs_status ogs_batch_free(ogs_batch b);
 
 /* Message of the calling thread's last failed call ("" if none). */
 const char *ogs_last_error_string(void);

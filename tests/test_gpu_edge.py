@@ -105,3 +105,4 @@ def test_bad_arguments_on_device_handle(cuda):
     assert L.ogs_gather_scatter(g.handle, d.data_ptr(), 1, 1, 9, 0, None) == _lib.OGS_EINVAL
     assert L.ogs_gather_scatter(g.handle, d.data_ptr(), 1, 1, 0, 5, None) == _lib.OGS_EINVAL
     assert L.ogs_gather_scatter(g.handle, None, 1, 1, 0, 0, None) == _lib.OGS_EINVAL
+

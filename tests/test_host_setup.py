@@ -71,3 +71,22 @@ def test_c2_box_counts_match_closed_form(oracle_mod):
     assert g.NgatherGlobal == cf["global"] == 4826809
     st = g.layout_stats()
     assert st["rows_by_degree"] == cf["rows_by_degree"] == {1: 3112136, 2: 1470804, 4: 231702, 8: 12167}
+
+
+@pytest.mark.parametrize("name", ["c1_box", "box_permuted", "random_multiplicity", "high_degree"])
+def test_host_pipeline_phases_are_safe(oracle_mod, name):
+    """The host-buffer pipeline copies node chunks in and out around slices of
+    the tiles; every slice must find its nodes already copied in, and no later
+    slice may touch nodes that were already copied out."""
+    ids = CASES[name]()
+    g = ogs.ogs_t().Setup(ids.size, ids.copy(), host_only=True)
+    ph = g.layout_stats()["phases"]
+    assert 1 <= len(ph) <= 8
+    assert ph[-1][2] == ids.size and ph[-1][3] == ids.size
+    prev_d = 0
+    for p, (lo, hi, h1, d1) in enumerate(ph):
+        assert hi < h1  # touched nodes are in chunks 0..p
+        assert d1 >= prev_d
+        for q in range(p + 1, len(ph)):
+            assert ph[q][0] >= d1  # later slices stay above the nodes sent back
+        prev_d = d1
