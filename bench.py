@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-meshes", type=int, default=256)
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--served-requests", type=int, default=20000)
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
@@ -232,6 +234,93 @@ def run_batched(a, dev, L, stream, log=None):
             "l2": "working set larger than L2 (no flush)", "graph": True}
 
 
+def run_served(a, dev, L, stream):
+    """Served gather-scatter: 64 resident meshes drawn like the batched mix; a
+    request picks a mesh uniformly, fp64 or fp32 (50/50), k uniform in [1,8],
+    op Add 80% / Min 10% / Max 10%, values U[-1,1] (integers are not used);
+    fields live in pinned host memory and are admitted against a 16 GB device
+    budget.  First a saturation run (all requests queued at once) gives the
+    throughput; then Poisson arrivals at 25%, 50% and 80% of it give p50/p99
+    latency, counted from each request's scheduled arrival.  Plain = the same
+    requests one after another through ogs_gather_scatter_host."""
+    import torch
+    from dawgs_gb300 import mesh, ogs
+    mix = mesh.mesh_mix(64, seed=77, lo=2, hi=16, pmax=7)
+    handles = []
+    for nx, ny, nz, p in mix:
+        ids = mesh.box_ids(nx, ny, nz, p)
+        handles.append(ogs.ogs_t().Setup(ids.size, ids, None, ogs.Unsigned))
+    n = a.served_requests
+    r = mesh.splitmix64(np.arange(4 * n, dtype=np.uint64) + np.uint64(4242))
+    meshes = (r[0::4] % np.uint64(64)).astype(np.int64)
+    dts = (r[1::4] % np.uint64(2)).astype(np.int64)            # 0: fp64, 1: fp32
+    ks = 1 + (r[2::4] % np.uint64(8)).astype(np.int64)
+    u = (r[3::4] % np.uint64(10)).astype(np.int64)
+    ops = np.where(u < 8, 0, np.where(u == 8, 3, 2))           # Add / Min / Max
+    nodes = np.array([handles[m].N for m in meshes], np.int64)
+    nbytes = nodes * ks * np.where(dts == 0, 8, 4)
+    dofs = float(sum(handles[m].NgatherGlobal * k for m, k in zip(meshes, ks)))
+    # one pinned arena; request i works in place on its own slice, reused round-robin
+    arena_bytes = int(max(256 << 20, 2 * nbytes.max()))
+    arena = torch.empty(arena_bytes // 8, dtype=torch.float64).pin_memory()
+    arena.uniform_(-1.0, 1.0)
+    offs, off = np.zeros(n, np.int64), 0
+    for i in range(n):
+        b = int(nbytes[i])
+        if off + b > arena_bytes:
+            off = 0
+        offs[i] = off
+        off += (b + 255) // 256 * 256
+    views = []
+    for i in range(n):
+        t = torch.float64 if dts[i] == 0 else torch.float32
+        cnt = int(nodes[i] * ks[i])
+        views.append(arena.view(torch.uint8)[offs[i]:offs[i] + nbytes[i]].view(t)[:cnt])
+
+    def serve(rate):
+        srv = ogs.ogs_server_t(field_budget_bytes=16 << 30, max_inflight=4096, max_batch=256)
+        for g in handles:
+            srv.add_mesh(g)
+        t0 = srv.clock() + 0.01
+        if rate is None:
+            arr = np.full(n, t0)
+        else:
+            gaps = -np.log(1.0 - (mesh.splitmix64(np.arange(n, dtype=np.uint64) + np.uint64(99)) >> np.uint64(11))
+                           .astype(np.float64) / 9007199254740992.0) / rate
+            arr = t0 + np.cumsum(gaps)
+        for i in range(n):
+            while rate is not None and srv.clock() < arr[i]:
+                pass
+            srv.submit(int(meshes[i]), views[i], int(ks[i]), int(ops[i]), 0, arrival=float(arr[i]))
+        srv.drain()
+        ta, td = srv.times(0, n)
+        launches, _ = srv.counters()
+        srv.Free()
+        lat = (td - ta) * 1e3
+        span = td.max() - ta.min()
+        return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "dofs_per_s": dofs / span, "requests_per_s": n / span, "launches": int(launches)}
+
+    sat = serve(None)
+    rates = {}
+    for frac in (0.25, 0.5, 0.8):
+        rates[f"{int(frac * 100)}%"] = dict(serve(frac * sat["requests_per_s"]),
+                                             offered_per_s=frac * sat["requests_per_s"])
+    # plain: one host-buffer call per request, back to back
+    m_plain = min(n, 4000)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for i in range(m_plain):
+        handles[meshes[i]].GatherScatter(views[i], int(ks[i]), int(ops[i]), 0, stream=stream)
+    t_plain = time.perf_counter() - t0
+    dofs_plain = float(sum(handles[meshes[i]].NgatherGlobal * ks[i] for i in range(m_plain)))
+    return {"workload": "64 resident box meshes (NX,NY,NZ~U[2,16], p~U[1,7]); requests fp64/fp32 50/50, "
+                        "k~U[1,8], Add 80%/Min 10%/Max 10%, pinned host fields, 16 GB device budget",
+            "requests": n, "saturation": sat, "poisson": rates,
+            "plain_dofs_per_s": dofs_plain / t_plain, "plain_requests": m_plain,
+            "speedup_vs_plain": sat["dofs_per_s"] / (dofs_plain / t_plain)}
+
+
 # ------------------------------------------------------------------ arms
 def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
@@ -372,6 +461,9 @@ def run_ours(a):
     batched = None
     if rank == 0 and world == 1 and not a.no_batched:
         batched = run_batched(a, dev, L, stream)
+    served = None
+    if rank == 0 and world == 1 and not a.no_served:
+        served = run_served(a, dev, L, stream)
 
     peak, peak_src = hbm_peak()
     nbytes_alg = alg_bytes(ids.size, g.nnzT, g.NlocalT, a.k, s)
@@ -396,6 +488,7 @@ def run_ours(a):
         "cpu_baseline": cpu,
         "e2e": e2e,
         "batched": batched,
+        "served": served,
         "gpu_launches": a.steps,
         "clocks": clk.summary(),
         "wall_ms_per_step_incl_restore_and_flush": 1e3 * (w1 - w0) / a.steps,

@@ -42,6 +42,15 @@ SIGNATURES = {
     "ogs_batch_tune": (_i, [_vp, _vp, _vp]),
     "ogs_batch_items": (_i, [_vp, _vp]),
     "ogs_batch_free": (_i, [_vp]),
+    "ogs_server_create": (_i, [C.POINTER(_vp), _vp]),
+    "ogs_server_add_mesh": (_i, [_vp, _vp, _vp]),
+    "ogs_server_submit": (_i, [_vp, _vp, C.c_double, _vp]),
+    "ogs_server_clock": (C.c_double, []),
+    "ogs_server_wait": (_i, [_vp, _i64]),
+    "ogs_server_drain": (_i, [_vp]),
+    "ogs_server_latencies": (_i, [_vp, _i64, _i64, _vp, _vp]),
+    "ogs_server_counters": (_i, [_vp, _vp, _vp]),
+    "ogs_server_free": (_i, [_vp]),
     "ogs_last_error_string": (C.c_char_p, []),
     "ogs_version": (_i, []),
 }
@@ -66,6 +75,15 @@ class OgsBatchEntry(C.Structure):
 
 
 BATCH_GRAPH = 1
+
+
+class OgsServerConfig(C.Structure):
+    _fields_ = [("field_budget_bytes", C.c_int64), ("max_inflight", C.c_int32), ("max_batch", C.c_int32)]
+
+
+class OgsServerRequest(C.Structure):
+    _fields_ = [("mesh", C.c_int32), ("type", C.c_int32), ("k", C.c_int32), ("op", C.c_int32),
+                ("trans", C.c_int32), ("reserved", C.c_int32), ("host", C.c_void_p)]
 
 
 class OgsError(RuntimeError):

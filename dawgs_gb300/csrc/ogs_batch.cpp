@@ -136,7 +136,7 @@ ogs_status ogs_batch_create(ogs_batch* out, int type, const ogs_batch_entry* ent
     be.op = e.op;
     fill_pattern(e.h, e.trans, be);
     b->host_entries.push_back(be);
-    b->starts.push_back(b->starts.back() + e.h->dmaps.nwtiles);
+    b->starts.push_back(b->starts.back() + static_cast<int64_t>(e.h->dmaps.nwtiles) * e.k);
     if (e.h->dmaps.ngtiles > 0) b->general.push_back(i);
   }
   if ((s = cuda_err(cudaMalloc(&b->d_entries, sizeof(BatchEntry) * n), fn, "malloc")) != OGS_OK ||

@@ -3,12 +3,14 @@
 // A batch is a list of entries (mesh handle, field, k, op, transpose).  Each
 // handle carries, from setup, one 32-byte record per warp tile (WarpRec:
 // column and row arrays of its bucket, first row, degree and row count); the
-// batch adds a prefix table `starts` over the entries' record counts.  Warp w
-// of the grid takes records w, w+W, ... of the concatenated list, finds the
-// record's entry by binary search (in shared memory for up to kBatchSmem
-// entries), and runs the same per-warp pipeline as ogs_warp.cuh: the next
-// record's column ids load while the current record's k components are
-// gathered, folded and stored.  The fold follows ogsOperator.cpp:311-360 with
+// batch adds a prefix table `starts` over the entries' (record, component)
+// items.  Warp w of the grid takes items w, w+W, ..., finds an item's entry by
+// binary search (in shared memory for up to kBatchSmem entries), and runs the
+// same per-warp pipeline as ogs_warp.cuh: the next item's column ids load
+// while the current item's values are gathered, folded and stored.  The k
+// components of one record are neighbouring items, so they run on
+// neighbouring warps at the same time and share the column ids and field
+// sectors through L1/L2.  The fold follows ogsOperator.cpp:311-360 with
 // the entry's op chosen at run time (warp-uniform), so one launch serves
 // entries with different ops.
 #pragma once
@@ -54,6 +56,34 @@ __device__ __forceinline__ int batch_entry_of(const int64_t* starts, int n, int6
   return lo;
 }
 
+// One work item: (entry e, warp record r, component k).
+struct BatchItem {
+  BatchEntry e;
+  WarpRec w;
+  int32_t r, k;
+};
+
+__device__ __forceinline__ void batch_item(const BatchEntry* E, const int64_t* st, int n, int64_t i,
+                                           BatchItem& it) {
+  const int e = batch_entry_of(st, n, i);
+  it.e = E[e];
+  const int64_t local = i - st[e];
+  it.r = static_cast<int32_t>(local / it.e.K);
+  it.k = static_cast<int32_t>(local - static_cast<int64_t>(it.r) * it.e.K);
+  it.w = it.e.recs[it.r];
+}
+
+__device__ __forceinline__ void batch_load_state(const BatchItem& it, int lane, WarpState& s) {
+  const Pattern pat{it.e.gather_n, it.e.scatter_n, it.e.limit_n};
+  DevBucket b;
+  Tile t;
+#define OGS_B_LOAD(D) \
+  rec_to_tile<D>(it.w, b, t); \
+  warp_load_state<kModeGS, D>(b, t, it.e.wemask, it.r, it.e.use_mask, pat, lane, s)
+  OGS_DEGREE_SWITCH(it.w.bucket_count >> 16, OGS_B_LOAD)
+#undef OGS_B_LOAD
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_batch_kernel(const BatchEntry* __restrict__ E,
                                                                           const int64_t* __restrict__ starts,
@@ -70,85 +100,35 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_batch_kernel(const 
   int64_t i = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + (threadIdx.x >> 5);
   if (i >= nitems) return;
 
-  // current record: its entry, tile and column ids
-  int ecur = batch_entry_of(st, n, i);
-  BatchEntry bcur = E[ecur];
-  int64_t rcur = i - st[ecur];
-  WarpRec wcur = bcur.recs[rcur];
+  BatchItem cur, nxt;
+  batch_item(E, st, n, i, cur);
   WarpState scur;
-  {
-    const Pattern pat{bcur.gather_n, bcur.scatter_n, bcur.limit_n};
-    DevBucket b;
-    Tile t;
-#define OGS_B_LOAD_CUR(D) \
-  rec_to_tile<D>(wcur, b, t); \
-  warp_load_state<kModeGS, D>(b, t, bcur.wemask, static_cast<int>(rcur), bcur.use_mask, pat, lane, scur)
-    OGS_DEGREE_SWITCH(wcur.bucket_count >> 16, OGS_B_LOAD_CUR)
-#undef OGS_B_LOAD_CUR
-  }
-  // next record's entry and descriptor
-  int enxt = 0;
-  BatchEntry bnxt{};
-  int64_t rnxt = 0;
-  WarpRec wnxt{};
-  if (i + W < nitems) {
-    enxt = batch_entry_of(st, n, i + W);
-    bnxt = E[enxt];
-    rnxt = i + W - st[enxt];
-    wnxt = bnxt.recs[rnxt];
-  }
+  batch_load_state(cur, lane, scur);
+  if (i + W < nitems) batch_item(E, st, n, i + W, nxt);
 
   for (;;) {
     const bool more = i + W < nitems;
-    const int K = bcur.K;
-    if (lane == 0) {
-      FieldArgs fa{};
-      fa.v = bcur.v;
-      prefetch_ahead<T>(fa, K, wcur.pf_lo, wcur.pf_hi, wcur.pf_cols, wcur.pf_stride, wcur.pf_begin,
-                        wcur.pf_bucket_count);
-    }
-    const bool gmask = bcur.gather_n != 0, smask = bcur.scatter_n != 0;
-    const int d = wcur.bucket_count >> 16;
-    WarpState snxt;
-    int enn = 0;
-    BatchEntry bnn{};
-    int64_t rnn = 0;
-    WarpRec wnn{};
-    for (int k = 0; k < K; ++k) {
-      T* base = static_cast<T*>(bcur.v) + k;
-      T V[kWarpSlots];
+    const int K = cur.e.K, k = cur.k, d = cur.w.bucket_count >> 16;
+    const bool gmask = cur.e.gather_n != 0, smask = cur.e.scatter_n != 0;
+    T* base = static_cast<T*>(cur.e.v) + k;
+    T V[kWarpSlots];
 #define OGS_B_VALS(D) warp_load_vals<T, kModeGS, D>(scur, base, nullptr, K, K, k, gmask, lane, V)
-      OGS_DEGREE_SWITCH(d, OGS_B_VALS)
+    OGS_DEGREE_SWITCH(d, OGS_B_VALS)
 #undef OGS_B_VALS
-      if (k == 0 && more) {
-        const Pattern pat{bnxt.gather_n, bnxt.scatter_n, bnxt.limit_n};
-        DevBucket b;
-        Tile t;
-#define OGS_B_LOAD_NXT(D) \
-  rec_to_tile<D>(wnxt, b, t); \
-  warp_load_state<kModeGS, D>(b, t, bnxt.wemask, static_cast<int>(rnxt), bnxt.use_mask, pat, lane, snxt)
-        OGS_DEGREE_SWITCH(wnxt.bucket_count >> 16, OGS_B_LOAD_NXT)
-#undef OGS_B_LOAD_NXT
-        if (i + 2 * W < nitems) {
-          enn = batch_entry_of(st, n, i + 2 * W);
-          bnn = E[enn];
-          rnn = i + 2 * W - st[enn];
-          wnn = bnn.recs[rnn];
-        }
-      }
-#define OGS_B_FOLD(D) fold_store_rt<T, D>(bcur.op, scur, base, K, K, k, gmask, smask, lane, V)
-      OGS_DEGREE_SWITCH(d, OGS_B_FOLD)
-#undef OGS_B_FOLD
+    WarpState snxt;
+    BatchItem nn;
+    if (more) {
+      batch_load_state(nxt, lane, snxt);
+      if (i + 2 * W < nitems) batch_item(E, st, n, i + 2 * W, nn);
     }
+#define OGS_B_FOLD(D) fold_store_rt<T, D>(cur.e.op, scur, base, K, K, k, gmask, smask, lane, V)
+    OGS_DEGREE_SWITCH(d, OGS_B_FOLD)
+#undef OGS_B_FOLD
     if (!more) break;
     i += W;
-    bcur = bnxt;
-    rcur = rnxt;
-    wcur = wnxt;
+    cur = nxt;
     scur = snxt;
-    bnxt = bnn;
-    rnxt = rnn;
-    wnxt = wnn;
+    nxt = nn;
   }
 }
 

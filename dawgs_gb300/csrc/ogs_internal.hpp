@@ -28,12 +28,6 @@ constexpr int kTileNnz = 2048;
 constexpr int kEntriesPerThread = kTileNnz / kBlock;
 // General-bucket tiles hold at most one row per thread.
 constexpr int kGeneralRowsPerTile = kBlock;
-// A warp tile prefetches, into L2, what the tile this many positions later
-// in the sweep will read (about two waves of resident warps ahead; 0 = off).
-#ifndef OGS_PREFETCH_AHEAD
-#define OGS_PREFETCH_AHEAD 8192
-#endif
-constexpr int kPrefetchAhead = OGS_PREFETCH_AHEAD;
 // Separate arrays handled by one launch of the *_many entry points.
 constexpr int kMaxMany = 16;
 // Member entries per lane of a warp tile (ogs_warp.cuh): lane l owns
@@ -93,19 +87,14 @@ struct Tile {
 // One warp tile as a self-contained 32-byte record, for launches that walk
 // the tiles of several meshes (ogs_batch.cuh).
 struct WarpRec {
-  const int32_t* cols;     // the bucket's column ids (member q of row i at cols[q*stride + i])
-  const int32_t* rows;     // the bucket's row ids
-  const int32_t* pf_cols;  // column ids of the bucket of the tile prefetched for
-  int32_t begin;           // first bucket row of the tile
-  int32_t bucket_count;    // degree << 16 | rows in the tile
-  int32_t stride;          // the bucket's stride
-  int32_t nP;              // bucket rows below NrowsN
-  int32_t pf_lo, pf_hi;    // as WTile
-  int32_t pf_begin, pf_bucket_count;
-  int32_t pf_stride;
-  int32_t pad;
+  const int32_t* cols;   // the bucket's column ids (member q of row i at cols[q*stride + i])
+  const int32_t* rows;   // the bucket's row ids
+  int32_t begin;         // first bucket row of the tile
+  int32_t bucket_count;  // degree << 16 | rows in the tile
+  int32_t stride;        // the bucket's stride
+  int32_t nP;            // bucket rows below NrowsN
 };
-static_assert(sizeof(WarpRec) == 64, "WarpRec is 64 bytes");
+static_assert(sizeof(WarpRec) == 32, "WarpRec is 32 bytes");
 
 // One entry of a batched launch, in device memory.
 struct BatchEntry {
@@ -115,17 +104,10 @@ struct BatchEntry {
   int32_t K, op;
   int32_t gather_n, scatter_n, limit_n, use_mask;
 };
+// Work items of a batched launch: each (warp record, component) pair of each
+// entry; starts[e] = first item of entry e, records of an entry in order with
+// their K components adjacent.
 
-// A warp tile (ogs_warp.cuh) with the L2 prefetch it issues for the tile
-// kPrefetchAhead positions later: field nodes [pf_lo, pf_hi) that no earlier
-// tile has asked for, and the column-id chunks of that later tile.
-struct WTile {
-  int32_t bucket, begin, count, first_row;
-  int32_t pf_lo, pf_hi;      // node range, empty when pf_hi <= pf_lo
-  int32_t pf_begin;          // first bucket row of the later tile
-  int32_t pf_bucket_count;   // its degree << 16 | rows (0: none)
-};
-static_assert(sizeof(WTile) == 32, "WTile is 32 bytes");
 
 struct DevMaps {
   DevBucket b[kDmax + 1];  // b[0] unused
@@ -135,7 +117,7 @@ struct DevMaps {
   int32_t signed_maps;     // N maps differ from T maps
   int32_t ngtiles;         // general-bucket CTA tiles, ordered by first row
   const Tile* gtiles;
-  const WTile* wtiles;     // exact-degree warp tiles (ogs_warp.cuh), ordered by first row
+  const Tile* wtiles;      // exact-degree warp tiles (ogs_warp.cuh), ordered by first row
   const uint8_t* wemask;   // [nwtiles][32] per-lane entry masks of the N map (Signed only)
   int32_t nwtiles;
   const WarpRec* wrecs;    // [nwtiles] the warp tiles as records (batched launches)
@@ -181,7 +163,7 @@ struct HostLayout {
   int32_t g_nP = 0;
   std::vector<Tile> tiles;   // CTA tiles, all buckets, by first row
   std::vector<Tile> gtiles;  // general CTA tiles, by first row
-  std::vector<WTile> wtiles; // exact-degree warp tiles, by first row
+  std::vector<Tile> wtiles;  // exact-degree warp tiles, by first row
   std::vector<uint8_t> wemask;
   std::vector<Phase> phases;
 };
@@ -222,7 +204,6 @@ void build_layout(ogs_handle_s* h);
 ogs_status upload_layout(ogs_handle_s* h);
 void release_device(ogs_handle_s* h);
 void build_phases(ogs_handle_s* h, int max_phases);
-void build_prefetch(HostLayout& L, int ahead);
 // DevMaps restricted to the tiles of one phase.
 DevMaps phase_maps(const DevMaps& m, const Phase& p);
 

@@ -270,14 +270,13 @@ void build_layout(ogs_handle_s* h) {
     const int32_t n = static_cast<int32_t>(cnt[d]);
     const int32_t step = warp_rows_per_tile(d);
     for (int32_t i = 0; i < n; i += step)
-      L.wtiles.push_back(WTile{d, i, std::min(step, n - i), L.rows[d][i], 0, 0, 0, 0});
+      L.wtiles.push_back(Tile{d, i, std::min(step, n - i), L.rows[d][i]});
   }
-  std::stable_sort(L.wtiles.begin(), L.wtiles.end(),
-                   [](const WTile& a, const WTile& b) { return a.first_row < b.first_row; });
+  std::stable_sort(L.wtiles.begin(), L.wtiles.end(), by_row);
   L.wemask.assign(sgn ? L.wtiles.size() * 32 : 0, 0);
   if (sgn) {
     for (size_t t = 0; t < L.wtiles.size(); ++t) {
-      const WTile& w = L.wtiles[t];
+      const Tile& w = L.wtiles[t];
       const int d = w.bucket;
       for (int lane = 0; lane < 32; ++lane) {
         uint32_t bits = 0;
@@ -293,38 +292,7 @@ void build_layout(ogs_handle_s* h) {
   }
   L.tiles.insert(L.tiles.end(), L.gtiles.begin(), L.gtiles.end());
   std::stable_sort(L.tiles.begin(), L.tiles.end(), by_row);
-  build_prefetch(L, kPrefetchAhead);
   build_phases(h, 8);
-}
-
-// Tile t asks L2 for what tile t+ahead will read: the field nodes above the
-// highest node any tile before it reaches, and its column-id chunks.  Tiles
-// are in row (first appearance) order, so the highest node reached grows
-// with t and every node is asked for once.
-void build_prefetch(HostLayout& L, int ahead) {
-  const int64_t nw = static_cast<int64_t>(L.wtiles.size());
-  std::vector<int32_t> cummax(nw);
-  int32_t run = -1;
-  for (int64_t t = 0; t < nw; ++t) {
-    const WTile& w = L.wtiles[t];
-    const int d = w.bucket;
-    const int64_t stride = static_cast<int64_t>(L.rows[d].size());
-    for (int q = 0; q < d; ++q)
-      for (int32_t r = 0; r < w.count; ++r) run = std::max(run, L.cols[d][q * stride + w.begin + r]);
-    cummax[t] = run;
-  }
-  for (int64_t t = 0; t < nw; ++t) {
-    WTile& w = L.wtiles[t];
-    const int64_t u = t + ahead;
-    if (ahead <= 0 || u >= nw) {
-      w.pf_lo = w.pf_hi = w.pf_begin = w.pf_bucket_count = 0;
-      continue;
-    }
-    w.pf_lo = cummax[u - 1] + 1;
-    w.pf_hi = cummax[u] + 1;
-    w.pf_begin = L.wtiles[u].begin;
-    w.pf_bucket_count = (L.wtiles[u].bucket << 16) | L.wtiles[u].count;
-  }
 }
 
 void build_phases(ogs_handle_s* h, int max_phases) {
@@ -353,7 +321,7 @@ void build_phases(ogs_handle_s* h, int max_phases) {
     ph.g1 = g;
     int64_t lo = INT64_MAX, hi = -1;
     for (int32_t t = ph.w0; t < ph.w1; ++t) {
-      const WTile& w = L.wtiles[t];
+      const Tile& w = L.wtiles[t];
       const int d = w.bucket;
       const int64_t stride = static_cast<int64_t>(L.rows[d].size());
       for (int q = 0; q < d; ++q)
@@ -447,7 +415,7 @@ ogs_status upload_layout(ogs_handle_s* h) {
   const size_t o_gcN = sgn ? add(L.g_colsN.data(), L.g_colsN.size() * 4) : o_gcT;
   const size_t o_tiles = add(L.tiles.data(), L.tiles.size() * sizeof(Tile));
   const size_t o_gtiles = add(L.gtiles.data(), L.gtiles.size() * sizeof(Tile));
-  const size_t o_wtiles = add(L.wtiles.data(), L.wtiles.size() * sizeof(WTile));
+  const size_t o_wtiles = add(L.wtiles.data(), L.wtiles.size() * sizeof(Tile));
   const size_t o_wemask = add(L.wemask.data(), L.wemask.size());
   // warp records hold device pointers: filled in once the arena exists
   std::vector<WarpRec> wrecs(L.wtiles.size());
@@ -464,7 +432,7 @@ ogs_status upload_layout(ogs_handle_s* h) {
                      std::string("cudaMalloc of maps: ") + cudaGetErrorString(e));
   }
   for (size_t t = 0; t < L.wtiles.size(); ++t) {
-    const WTile& w = L.wtiles[t];
+    const Tile& w = L.wtiles[t];
     WarpRec& r = wrecs[t];
     r.cols = reinterpret_cast<const int32_t*>(base + o_cols[w.bucket]);
     r.rows = reinterpret_cast<const int32_t*>(base + o_rows[w.bucket]);
@@ -472,14 +440,6 @@ ogs_status upload_layout(ogs_handle_s* h) {
     r.bucket_count = (w.bucket << 16) | w.count;
     r.stride = static_cast<int32_t>(L.rows[w.bucket].size());
     r.nP = L.nP[w.bucket];
-    r.pf_lo = w.pf_lo;
-    r.pf_hi = w.pf_hi;
-    r.pf_begin = w.pf_begin;
-    r.pf_bucket_count = w.pf_bucket_count;
-    const int pd = w.pf_bucket_count >> 16;
-    r.pf_cols = pd ? reinterpret_cast<const int32_t*>(base + o_cols[pd]) : nullptr;
-    r.pf_stride = pd ? static_cast<int32_t>(L.rows[pd].size()) : 0;
-    r.pad = 0;
   }
   for (const Piece& p : pieces) {
     if (!p.bytes) continue;
@@ -513,7 +473,7 @@ ogs_status upload_layout(ogs_handle_s* h) {
   m.ntiles = static_cast<int32_t>(L.tiles.size());
   m.gtiles = reinterpret_cast<const Tile*>(base + o_gtiles);
   m.ngtiles = static_cast<int32_t>(L.gtiles.size());
-  m.wtiles = reinterpret_cast<const WTile*>(base + o_wtiles);
+  m.wtiles = reinterpret_cast<const Tile*>(base + o_wtiles);
   m.nwtiles = static_cast<int32_t>(L.wtiles.size());
   m.wemask = reinterpret_cast<const uint8_t*>(base + o_wemask);
   m.wrecs = reinterpret_cast<const WarpRec*>(base + o_wrecs);

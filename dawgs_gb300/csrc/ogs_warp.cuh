@@ -41,8 +41,8 @@ struct WarpState {
   int32_t cnt;              // rows of the tile this call processes
 };
 
-template <int MODE, int D, typename TileT>
-__device__ __forceinline__ void warp_load_state(const DevBucket& b, const TileT& t, const uint8_t* wemask,
+template <int MODE, int D>
+__device__ __forceinline__ void warp_load_state(const DevBucket& b, const Tile& t, const uint8_t* wemask,
                                                 int tile_index, bool use_mask, const Pattern& pat, int lane,
                                                 WarpState& s) {
   constexpr int RPT = warp_rows_per_lane(D);
@@ -105,47 +105,6 @@ __device__ __forceinline__ void warp_fold_store(const WarpState& s, T* dst, T* g
   }
 }
 
-// Asynchronous bulk prefetch of global bytes [a, b) into L2 (the TMA unit's
-// prefetch; no completion to wait for).  The range is shrunk to 16-byte
-// boundaries, as the instruction requires, so it never leaves the buffer.
-__device__ __forceinline__ void l2_prefetch(const void* a, const void* b) {
-  uintptr_t lo = (reinterpret_cast<uintptr_t>(a) + 15) & ~uintptr_t(15);
-  const uintptr_t hi = reinterpret_cast<uintptr_t>(b) & ~uintptr_t(15);
-  while (lo < hi) {
-    const uint32_t n = static_cast<uint32_t>(hi - lo < 65536 ? hi - lo : 65536);
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"(n) : "memory");
-    lo += n;
-  }
-}
-
-// What a tile prefetches for the tile kPrefetchAhead positions later: the
-// field nodes [pf_lo, pf_hi) of every component array and that tile's
-// column-id chunks.
-template <typename T>
-__device__ __forceinline__ void prefetch_ahead(const FieldArgs& f, int K, int32_t pf_lo, int32_t pf_hi,
-                                               const int32_t* pf_cols, int32_t pf_stride, int32_t pf_begin,
-                                               int32_t pf_bucket_count) {
-  if (pf_hi > pf_lo) {
-    if (f.is_many) {
-      for (int k = 0; k < K; ++k) {
-        const T* a = static_cast<const T*>(f.many[k]);
-        l2_prefetch(a + pf_lo, a + pf_hi);
-      }
-    } else {
-      const T* a = static_cast<const T*>(f.v);
-      l2_prefetch(a + static_cast<int64_t>(pf_lo) * K, a + static_cast<int64_t>(pf_hi) * K);
-    }
-  }
-  const int pd = pf_bucket_count >> 16, pc = pf_bucket_count & 0xFFFF;
-  if (pd && pf_cols) {
-    const int32_t n4 = (pc + 3) & ~3;
-    for (int q = 0; q < pd; ++q) {
-      const int32_t* c = pf_cols + static_cast<int64_t>(q) * pf_stride + pf_begin;
-      l2_prefetch(c, c + n4);
-    }
-  }
-}
-
 #define OGS_DEGREE_SWITCH(bucket, CALL) \
   switch (bucket) {                     \
     case 1: CALL(1); break;             \
@@ -172,25 +131,17 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const D
   const int64_t stride = K1 ? 1 : (f.is_many ? 1 : K);
 
   int tcur = static_cast<int>(i / K);
-  WTile cur = m.wtiles[tcur];
+  Tile cur = m.wtiles[tcur];
   WarpState scur;
 #define OGS_LOAD_CUR(D) warp_load_state<MODE, D>(m.b[D], cur, m.wemask, tcur, use_mask, pat, lane, scur)
   OGS_DEGREE_SWITCH(cur.bucket, OGS_LOAD_CUR)
 #undef OGS_LOAD_CUR
-  WTile nxt{};
+  Tile nxt{};
   if (i + W < nitems) nxt = m.wtiles[(i + W) / K];
 
   for (;;) {
     const int k = K1 ? 0 : static_cast<int>(i % K);
-    if (lane == 0 && k == 0 && MODE != kModeScatter) {
-      const int pd = cur.pf_bucket_count >> 16;
-      const int32_t* pcols = nullptr;
-      int32_t pstride = 0;
-#define OGS_PF_COLS(D) pcols = m.b[D].cols; pstride = m.b[D].stride
-      if (pd) { OGS_DEGREE_SWITCH(pd, OGS_PF_COLS) }
-#undef OGS_PF_COLS
-      prefetch_ahead<T>(f, K, cur.pf_lo, cur.pf_hi, pcols, pstride, cur.pf_begin, cur.pf_bucket_count);
-    }
+
     const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, k);
     T* dst = (MODE == kModeGather) ? nullptr : field_base<T>(f, k);
     T* gv = static_cast<T*>(f.gv);
@@ -200,7 +151,7 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const D
 #undef OGS_VALS
     const bool more = i + W < nitems;
     WarpState snxt;
-    WTile nn{};
+    Tile nn{};
     int tnxt = 0;
     if (more) {
       tnxt = static_cast<int>((i + W) / K);

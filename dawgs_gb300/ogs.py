@@ -283,3 +283,60 @@ class ogs_batch_t:
             self.Free()
         except Exception:
             pass
+
+
+class ogs_server_t:
+    """Served gather-scatter (no reference counterpart): resident meshes,
+    requests admitted against an HBM budget, continuous batching."""
+
+    def __init__(self, field_budget_bytes=16 << 30, max_inflight=4096, max_batch=256):
+        cfg = _lib.OgsServerConfig(int(field_budget_bytes), int(max_inflight), int(max_batch))
+        s = C.c_void_p()
+        check(lib().ogs_server_create(C.byref(s), C.byref(cfg)))
+        self._s = s
+        self.meshes = []
+
+    def add_mesh(self, g: ogs_t) -> int:
+        mid = C.c_int()
+        check(lib().ogs_server_add_mesh(self._s, g.handle, C.byref(mid)))
+        self.meshes.append(g)
+        return mid.value
+
+    def submit(self, mesh: int, host, k: int, op=Add, trans=Sym, arrival: float = 0.0) -> int:
+        t = _type_of(host)
+        r = _lib.OgsServerRequest(int(mesh), int(t), int(k), int(op), int(trans), 0, _ptr(host))
+        rid = C.c_int64()
+        check(lib().ogs_server_submit(self._s, C.byref(r), float(arrival), C.byref(rid)))
+        return rid.value
+
+    @staticmethod
+    def clock() -> float:
+        return float(lib().ogs_server_clock())
+
+    def wait(self, rid: int):
+        check(lib().ogs_server_wait(self._s, int(rid)))
+
+    def drain(self):
+        check(lib().ogs_server_drain(self._s))
+
+    def times(self, first: int, n: int):
+        a = np.zeros(n)
+        d = np.zeros(n)
+        check(lib().ogs_server_latencies(self._s, int(first), int(n), a.ctypes.data, d.ctypes.data))
+        return a, d
+
+    def counters(self):
+        l, b = C.c_int64(), C.c_int64()
+        check(lib().ogs_server_counters(self._s, C.byref(l), C.byref(b)))
+        return l.value, b.value
+
+    def Free(self):
+        if getattr(self, "_s", None) is not None and _lib._lib is not None:
+            lib().ogs_server_free(self._s)
+        self._s = None
+
+    def __del__(self):
+        try:
+            self.Free()
+        except Exception:
+            pass

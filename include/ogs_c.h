@@ -158,9 +158,50 @@ ogs_status ogs_batch_gather_scatter(ogs_batch b, void *stream);
 /* Time the candidate launch shapes (1..6 persistent CTAs per SM) on the
  * batch's own fields -- which they update in place -- and keep the fastest. */
 ogs_status ogs_batch_tune(ogs_batch b, void *stream, int *chosen_grid);
-/* Warp tiles the batched launch walks. */
+/* Work items (warp tile x component) the batched launch walks. */
 ogs_status ogs_batch_items(ogs_batch b, int64_t *items);
 ogs_status ogs_batch_free(ogs_batch b);
+
+/* ---- Served gather-scatter: resident meshes, continuous batching ----
+ * No reference counterpart.  Requests name a resident mesh and carry a host
+ * field (k interleaved components per node), gather-scattered in place with
+ * the request's op and transpose.  A worker thread admits pending requests in
+ * arrival order while a device buffer for the field fits in the budget and an
+ * in-flight slot is free, copies them in, runs everything admitted since its
+ * last turn as one batched launch per value type (alternating between two
+ * compute streams, so batches overlap on the GPU), copies results back and
+ * retires them.  Each result equals ogs_gather_scatter_host of that request
+ * alone, bit for bit.  Submit from any thread; the host field must stay valid
+ * and untouched until the request completes. */
+typedef struct ogs_server_s *ogs_server;
+typedef struct {
+  int64_t field_budget_bytes; /* device memory for request fields (the HBM budget) */
+  int32_t max_inflight;       /* requests admitted and not yet retired */
+  int32_t max_batch;          /* requests per batched launch */
+} ogs_server_config;
+typedef struct {
+  int32_t mesh;   /* from ogs_server_add_mesh */
+  int32_t type;   /* ogs_type */
+  int32_t k;
+  int32_t op;     /* ogs_op */
+  int32_t trans;  /* ogs_transpose */
+  int32_t reserved;
+  void *host;     /* k*N values, in place */
+} ogs_server_request;
+ogs_status ogs_server_create(ogs_server *out, const ogs_server_config *cfg);
+/* Make a set-up handle resident (the server does not own it). */
+ogs_status ogs_server_add_mesh(ogs_server s, ogs_handle h, int *mesh_id);
+/* arrival: time on ogs_server_clock() the request arrived, or 0 for now. */
+ogs_status ogs_server_submit(ogs_server s, const ogs_server_request *r, double arrival, int64_t *id);
+double ogs_server_clock(void);
+ogs_status ogs_server_wait(ogs_server s, int64_t id);
+ogs_status ogs_server_drain(ogs_server s);
+/* Arrival and completion times (ogs_server_clock seconds; -1 = not done) of
+ * requests first..first+n-1. */
+ogs_status ogs_server_latencies(ogs_server s, int64_t first, int64_t n, double *arrival, double *done);
+ogs_status ogs_server_counters(ogs_server s, int64_t *launches, int64_t *batched_requests);
+/* Finishes outstanding requests, then releases the server. */
+ogs_status ogs_server_free(ogs_server s);
 
 /* Message of the calling thread's last failed call ("" if none). */
 const char *ogs_last_error_string(void);
