@@ -33,6 +33,7 @@ SIGNATURES = {
     "ogs_gather_scatter_host": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),
     "ogs_gather_host": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _vp]),
     "ogs_scatter_host": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp]),
+    "ogs_gather_scatter_host_noalloc": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),
     "ogs_get_counts": (_i, [_vp, _vp]),
     "ogs_get_maps": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "ogs_get_layout_stats": (_i, [_vp, _vp]),

@@ -124,6 +124,22 @@ ogs_status ogs_gather_host(ogs_handle h, void *gv, const void *v, int k, int typ
 ogs_status ogs_scatter_host(ogs_handle h, void *v, const void *gv, int k, int type, int trans,
                             void *stream);
 
+/* ogs_gather_scatter_host without any device allocation.  No counterpart in
+ * the reference: it exists for callers that must not have a library allocate
+ * device memory once they are running -- latency-critical loops (cudaMalloc
+ * and cudaFree synchronise the device), programs whose device memory belongs
+ * to a framework's caching allocator, services with a fixed memory footprint.
+ * The field is staged in a 32 MiB device array built into the library (held on
+ * every device that loads it, until exit) instead of a cudaMalloc'd buffer;
+ * fields larger than 32 MiB (N*k*sizeof(T)) are rejected with OGS_ERANGE.
+ * The first call on each device looks the array's address up (set-up); make
+ * that first call before any stream capture begins.  All calls share the one
+ * array: calls that overlap on the GPU race.  Nothing in it needs to start
+ * at zero: each call copies its whole field in before the kernel reads it.
+ * Same results as ogs_gather_scatter_host, bit for bit. */
+ogs_status ogs_gather_scatter_host_noalloc(ogs_handle h, void *v, int k, int type, int op, int trans,
+                                           void *stream);
+
 /* Counts of ogsBase_t (include/ogs/ogsBase.hpp:50-58). */
 ogs_status ogs_get_counts(ogs_handle h, ogs_counts *out);
 /* Host copies of the CSR maps of ogsOperator_t (include/ogs/ogsOperator.hpp:47-57):
