@@ -37,7 +37,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "ogs_tiles_kernel_gs_fp64_add_24x24x24_p7.md")
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "ogs_warp_kernel_gs_fp64_add_24x24x24_p7.md")
 FALLBACK_HBM_GBS = 6800.0
 TYPE_CODE = {"float32": 0, "float64": 1, "int32": 2, "int64": 3}
 OP_CODE = {"add": 0, "mul": 1, "max": 2, "min": 3}

@@ -21,19 +21,10 @@ namespace ogsgb {
 
 constexpr int kBatchSmem = 2048;
 
-template <int D>
-__device__ __forceinline__ void rec_to_tile(const WarpRec& r, DevBucket& b, Tile& t) {
-  b.cols = r.cols;
-  b.rows = r.rows;
-  b.nmask = nullptr;
-  b.n = 0;
-  b.nP = r.nP;
-  b.stride = r.stride;
-  t.bucket = D;
-  t.begin = r.begin;
-  t.count = r.bucket_count & 0xFFFF;
-  t.first_row = 0;
-}
+// Minimum resident CTAs per SM the batched kernel's registers must allow.
+#ifndef OGS_BATCH_MINB
+#define OGS_BATCH_MINB 2
+#endif
 
 template <typename T, int D>
 __device__ __forceinline__ void fold_store_rt(int op, const WarpState& s, T* dst, int64_t stride, int K, int k,
@@ -56,36 +47,57 @@ __device__ __forceinline__ int batch_entry_of(const int64_t* starts, int n, int6
   return lo;
 }
 
-// One work item: (entry e, warp record r, component k).
+// One work item, (entry e, warp record r, component k), reduced to what the
+// fold needs: field, masks, column ids of the record's bucket and its tile.
 struct BatchItem {
-  BatchEntry e;
-  WarpRec w;
+  const int32_t* cols;
+  void* v;
+  const uint8_t* wemask;
+  int32_t K, flags;  // flags: op | gather_n << 4 | scatter_n << 5 | limit_n << 6 | use_mask << 7
   int32_t r, k;
+  int32_t begin, bucket_count, stride, nP;
 };
 
 __device__ __forceinline__ void batch_item(const BatchEntry* E, const int64_t* st, int n, int64_t i,
                                            BatchItem& it) {
   const int e = batch_entry_of(st, n, i);
-  it.e = E[e];
+  const BatchEntry& be = E[e];
+  it.v = be.v;
+  it.wemask = be.wemask;
+  it.K = be.K;
+  it.flags = be.op | (be.gather_n << 4) | (be.scatter_n << 5) | (be.limit_n << 6) | (be.use_mask << 7);
   const int64_t local = i - st[e];
-  it.r = static_cast<int32_t>(local / it.e.K);
-  it.k = static_cast<int32_t>(local - static_cast<int64_t>(it.r) * it.e.K);
-  it.w = it.e.recs[it.r];
+  it.r = static_cast<int32_t>(local / it.K);
+  it.k = static_cast<int32_t>(local - static_cast<int64_t>(it.r) * it.K);
+  const WarpRec& w = be.recs[it.r];
+  it.cols = w.cols;
+  it.begin = w.begin;
+  it.bucket_count = w.bucket_count;
+  it.stride = w.stride;
+  it.nP = w.nP;
 }
 
 __device__ __forceinline__ void batch_load_state(const BatchItem& it, int lane, WarpState& s) {
-  const Pattern pat{it.e.gather_n, it.e.scatter_n, it.e.limit_n};
+  const Pattern pat{(it.flags >> 4) & 1, (it.flags >> 5) & 1, (it.flags >> 6) & 1};
   DevBucket b;
+  b.cols = it.cols;
+  b.rows = nullptr;
+  b.nmask = nullptr;
+  b.n = 0;
+  b.nP = it.nP;
+  b.stride = it.stride;
   Tile t;
-#define OGS_B_LOAD(D) \
-  rec_to_tile<D>(it.w, b, t); \
-  warp_load_state<kModeGS, D>(b, t, it.e.wemask, it.r, it.e.use_mask, pat, lane, s)
-  OGS_DEGREE_SWITCH(it.w.bucket_count >> 16, OGS_B_LOAD)
+  t.begin = it.begin;
+  t.count = it.bucket_count & 0xFFFF;
+  t.first_row = 0;
+  const bool use_mask = (it.flags >> 7) & 1;
+#define OGS_B_LOAD(D) t.bucket = D; warp_load_state<kModeGS, D>(b, t, it.wemask, it.r, use_mask, pat, lane, s)
+  OGS_DEGREE_SWITCH(it.bucket_count >> 16, OGS_B_LOAD)
 #undef OGS_B_LOAD
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_batch_kernel(const BatchEntry* __restrict__ E,
+__global__ void __launch_bounds__(kBlock, OGS_BATCH_MINB) ogs_batch_kernel(const BatchEntry* __restrict__ E,
                                                                           const int64_t* __restrict__ starts,
                                                                           int n) {
   __shared__ int64_t s_starts[kBatchSmem + 1];
@@ -108,9 +120,9 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_batch_kernel(const 
 
   for (;;) {
     const bool more = i + W < nitems;
-    const int K = cur.e.K, k = cur.k, d = cur.w.bucket_count >> 16;
-    const bool gmask = cur.e.gather_n != 0, smask = cur.e.scatter_n != 0;
-    T* base = static_cast<T*>(cur.e.v) + k;
+    const int K = cur.K, k = cur.k, d = cur.bucket_count >> 16;
+    const bool gmask = (cur.flags >> 4) & 1, smask = (cur.flags >> 5) & 1;
+    T* base = static_cast<T*>(cur.v) + k;
     T V[kWarpSlots];
 #define OGS_B_VALS(D) warp_load_vals<T, kModeGS, D>(scur, base, nullptr, K, K, k, gmask, lane, V)
     OGS_DEGREE_SWITCH(d, OGS_B_VALS)
@@ -121,7 +133,7 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_batch_kernel(const 
       batch_load_state(nxt, lane, snxt);
       if (i + 2 * W < nitems) batch_item(E, st, n, i + 2 * W, nn);
     }
-#define OGS_B_FOLD(D) fold_store_rt<T, D>(cur.e.op, scur, base, K, K, k, gmask, smask, lane, V)
+#define OGS_B_FOLD(D) fold_store_rt<T, D>(cur.flags & 15, scur, base, K, K, k, gmask, smask, lane, V)
     OGS_DEGREE_SWITCH(d, OGS_B_FOLD)
 #undef OGS_B_FOLD
     if (!more) break;

@@ -10,8 +10,9 @@
 //              copy-in stream and run as one batched launch per value type
 //              (ogs_batch.cuh) on the next of two compute streams, so a batch
 //              that arrives while another runs overlaps with it on the GPU;
-//   retire  -- each request's copy-out ends with a host callback that stamps
-//              its completion; the worker then returns its buffer to the pool.
+//   retire  -- each request's copy-out records an event; the worker polls the
+//              oldest outstanding events, stamps completions and returns the
+//              buffers to the pool.
 // Latency is completion minus arrival (the submit time, or the arrival time the
 // caller passes).  Every result equals the request's ogs_gather_scatter_host
 // alone, bit for bit: batching changes where the rows run, not their fold.
@@ -91,7 +92,7 @@ struct Req {
   size_t off = 0;
   double t_arrival = 0, t_done = 0;
   std::atomic<int> state{0};  // 0 pending, 1 in flight, 2 done
-  struct ogs_server_s* srv = nullptr;
+  cudaEvent_t copied_out = nullptr;
 };
 
 // Device tables of one batched launch, reused once its launch has finished.
@@ -124,8 +125,8 @@ struct ogs_server_s {
   std::condition_variable cv;
   std::deque<Req*> pending;
   std::vector<std::unique_ptr<Req>> all;  // by id
-  std::mutex done_mu;
-  std::vector<Req*> finished;            // filled by the completion callbacks
+  std::deque<Req*> outstanding;          // launched, in copy-out order (worker only)
+  std::vector<cudaEvent_t> spare_events; // recycled completion events (worker only)
   std::atomic<int64_t> inflight{0}, completed{0}, submitted{0};
   std::atomic<int64_t> launches{0}, batched_requests{0};
   std::thread worker;
@@ -135,19 +136,6 @@ struct ogs_server_s {
 
 namespace ogsgb {
 namespace {
-
-void CUDART_CB on_request_done(void* p) {
-  Req* q = static_cast<Req*>(p);
-  q->t_done = now_s();
-  q->state.store(2);
-  ogs_server_s* s = q->srv;
-  {
-    std::lock_guard<std::mutex> g(s->done_mu);
-    s->finished.push_back(q);
-  }
-  s->completed.fetch_add(1);
-  s->cv.notify_all();
-}
 
 int batch_launch(int type, const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, cudaStream_t st) {
   switch (type) {
@@ -217,25 +205,48 @@ int launch_group(ogs_server_s* s, const std::vector<Req*>& grp, int type, cudaEv
   for (int i = 0; !e && i < n; ++i) {
     Req* q = grp[i];
     e = cudaMemcpyAsync(q->r.host, s->pool_base + q->off, q->bytes, cudaMemcpyDeviceToHost, s->copy_out);
-    if (!e) e = cudaLaunchHostFunc(s->copy_out, on_request_done, q);
+    if (!e) {
+      if (s->spare_events.empty()) {
+        cudaEvent_t ev = nullptr;
+        e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (!e) s->spare_events.push_back(ev);
+      }
+    }
+    if (!e) {
+      q->copied_out = s->spare_events.back();
+      s->spare_events.pop_back();
+      e = cudaEventRecord(q->copied_out, s->copy_out);
+      s->outstanding.push_back(q);
+    }
   }
   s->launches.fetch_add(1);
   s->batched_requests.fetch_add(n);
   return e;
 }
 
+// Completions arrive in copy-out order: poll from the oldest.
 void retire(ogs_server_s* s) {
-  std::vector<Req*> fin;
-  {
-    std::lock_guard<std::mutex> g(s->done_mu);
-    fin.swap(s->finished);
+  int n = 0;
+  while (!s->outstanding.empty()) {
+    Req* q = s->outstanding.front();
+    const cudaError_t e = cudaEventQuery(q->copied_out);
+    if (e == cudaErrorNotReady) break;
+    const double t = now_s();
+    s->outstanding.pop_front();
+    s->spare_events.push_back(q->copied_out);
+    q->copied_out = nullptr;
+    {
+      std::lock_guard<std::mutex> g(s->mu);
+      if (e != cudaSuccess && s->error.empty()) s->error = cudaGetErrorString(e);
+      s->pool.release(q->off, q->bytes);
+      q->t_done = t;
+      q->state.store(2);
+      s->inflight.fetch_sub(1);
+    }
+    s->completed.fetch_add(1);
+    n++;
   }
-  if (fin.empty()) return;
-  std::lock_guard<std::mutex> g(s->mu);
-  for (Req* q : fin) {
-    s->pool.release(q->off, q->bytes);
-    s->inflight.fetch_sub(1);
-  }
+  if (n) s->cv.notify_all();
 }
 
 void worker_loop(ogs_server_s* s) {
@@ -247,10 +258,7 @@ void worker_loop(ogs_server_s* s) {
     retire(s);
     {
       std::unique_lock<std::mutex> lk(s->mu);
-      if (s->pending.empty() && admitted.empty()) {
-        if (s->stop.load() && s->inflight.load() == 0) break;
-        s->cv.wait_for(lk, std::chrono::microseconds(200));
-      }
+      if (s->pending.empty() && s->stop.load() && s->inflight.load() == 0) break;
       // admission: FIFO against the budget and the in-flight slots
       while (!s->pending.empty() && s->inflight.load() < s->cfg.max_inflight &&
              static_cast<int>(admitted.size()) < s->cfg.max_batch) {
@@ -261,8 +269,13 @@ void worker_loop(ogs_server_s* s) {
         s->inflight.fetch_add(1);
         admitted.push_back(q);
       }
+      if (admitted.empty()) {
+        // nothing to launch: wait for a submission, or come back soon to
+        // retire what is in flight (which may free budget for the pending)
+        s->cv.wait_for(lk, std::chrono::microseconds(s->outstanding.empty() ? 500 : 20));
+        continue;
+      }
     }
-    if (admitted.empty()) continue;
     int e = 0;
     for (Req* q : admitted)
       if (!e) e = cudaMemcpyAsync(s->pool_base + q->off, q->r.host, q->bytes, cudaMemcpyHostToDevice, s->copy_in);
@@ -283,6 +296,7 @@ void worker_loop(ogs_server_s* s) {
 }
 
 void destroy(ogs_server_s* s) {
+  for (cudaEvent_t ev : s->spare_events) cudaEventDestroy(ev);
   for (TableSlot& t : s->slots) {
     if (t.d_entries) cudaFree(t.d_entries);
     if (t.d_starts) cudaFree(t.d_starts);
@@ -361,7 +375,6 @@ ogs_status ogs_server_submit(ogs_server s, const ogs_server_request* r, double a
     if (q->bytes > static_cast<size_t>(s->cfg.field_budget_bytes))
       return set_error(OGS_ERANGE, "ogs_server_submit: the field is larger than the whole budget");
     q->t_arrival = arrival > 0 ? arrival : now_s();
-    q->srv = s;
     q->id = static_cast<int64_t>(s->all.size());
     if (id) *id = q->id;
     s->pending.push_back(q.get());
