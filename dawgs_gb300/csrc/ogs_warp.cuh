@@ -33,6 +33,24 @@
 
 namespace ogsgb {
 
+// GatherScatter skips the store to a member whose value already has the
+// result's bits: degree-1 rows under Add (x + 0 == x), the member holding the
+// maximum under Max, and so on.  Memory ends bit-identical to storing every
+// member; the store traffic of those members disappears.  OGS_SILENT_STORE=0
+// stores every member (for comparisons).
+#ifndef OGS_SILENT_STORE
+#define OGS_SILENT_STORE 1
+#endif
+
+template <typename T>
+__device__ __forceinline__ bool same_bits(const T a, const T b) {
+  using U = typename std::conditional<sizeof(T) == 8, unsigned long long, unsigned int>::type;
+  U x, y;
+  memcpy(&x, &a, sizeof(T));
+  memcpy(&y, &b, sizeof(T));
+  return x == y;
+}
+
 // Column ids, row ids and the per-lane entry mask of one warp tile.
 struct WarpState {
   int32_t I[kWarpSlots];  // entry e = j*D + q: member q of the lane's row j
@@ -98,8 +116,13 @@ __device__ __forceinline__ void warp_fold_store(const WarpState& s, T* dst, T* g
         gv[static_cast<int64_t>(s.R[j]) * K + k] = a;
       } else {
 #pragma unroll
-        for (int q = 0; q < D; ++q)
-          if (!smask || ((s.emask >> (j * D + q)) & 1u)) dst[static_cast<int64_t>(s.I[j * D + q]) * stride] = a;
+        for (int q = 0; q < D; ++q) {
+          const bool in_n = (s.emask >> (j * D + q)) & 1u;
+          if (smask && !in_n) continue;
+          // a member that took part in the fold still holds its value in V
+          if (OGS_SILENT_STORE && MODE == kModeGS && (!gmask || in_n) && same_bits(a, V[j * D + q])) continue;
+          dst[static_cast<int64_t>(s.I[j * D + q]) * stride] = a;
+        }
       }
     }
   }
