@@ -321,6 +321,20 @@ def run_served(a, dev, L, stream):
             "speedup_vs_plain": sat["dofs_per_s"] / (dofs_plain / t_plain)}
 
 
+def aggregate_over_ranks(seconds, units, device=None):
+    """Replicas: the job's time is the slowest rank's, its work the sum of all
+    ranks' units.  Returns (seconds, units, throughput)."""
+    import torch
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+        u = torch.tensor([float(units)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+        seconds, units = float(t.item()), float(u.item())
+    return seconds, units, units / seconds
+
+
 # ------------------------------------------------------------------ arms
 def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
@@ -362,6 +376,12 @@ def run_ours(a):
     from dawgs_gb300 import _lib, ogs
     ids, v = make_inputs(a)
     g = ogs.ogs_t().Setup(ids.size, ids.copy(), None, ogs.Unsigned, ogs.Auto, False)
+    # setup wall time, maps built on the GPU (the default at this size) and on the host
+    setup_s = {"local_dofs": int(ids.size)}
+    for how in ("device", "host"):
+        t0 = time.perf_counter()
+        ogs.ogs_t().Setup(ids.size, ids.copy(), None, ogs.Unsigned, ogs.Auto, False, maps=how).Free()
+        setup_s[f"{how}_maps_s"] = time.perf_counter() - t0
     tcode, ocode = TYPE_CODE[a.dtype], OP_CODE[a.op]
     s = np.dtype(a.dtype).itemsize
     pristine = torch.from_numpy(v).to(dev)
@@ -407,13 +427,8 @@ def run_ours(a):
         barrier()
         w1 = time.perf_counter()
     kt = [e0.elapsed_time(e1) * 1e-3 for e0, e1 in evs]
-    t_kernel = sum(kt)
-    if world > 1:
-        tt = torch.tensor([t_kernel], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_kernel = float(tt.item())
+    t_kernel, _, value = aggregate_over_ranks(sum(kt), g.NgatherGlobal * a.steps, dev)
     per_step = t_kernel / a.steps
-    value = world * g.NgatherGlobal * a.steps / t_kernel
 
     # e2e through the C ABI host-buffer entry point, pinned host memory
     e2e = None
@@ -430,13 +445,9 @@ def run_ours(a):
             t0 = time.perf_counter()
             _lib.check(L.ogs_gather_scatter_host(h, host.data_ptr(), a.k, tcode, ocode, 0, stream.cuda_stream))
             et.append(time.perf_counter() - t0)
-        t_e2e = sum(et)
-        if world > 1:
-            tt = torch.tensor([t_e2e], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            t_e2e = float(tt.item())
+        t_e2e, _, e2e_value = aggregate_over_ranks(sum(et), g.NgatherGlobal * a.steps, dev)
         nbytes = a.k * ids.size * s
-        e2e = {"value": world * g.NgatherGlobal * a.steps / t_e2e, "unit": "DOFS/s",
+        e2e = {"value": e2e_value, "unit": "DOFS/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "ms_per_step": 1e3 * t_e2e / a.steps, "api": "ogs_gather_scatter_host (C ABI)"}
 
@@ -489,6 +500,7 @@ def run_ours(a):
         "e2e": e2e,
         "batched": batched,
         "served": served,
+        "setup": setup_s,
         "gpu_launches": a.steps,
         "clocks": clk.summary(),
         "wall_ms_per_step_incl_restore_and_flush": 1e3 * (w1 - w0) / a.steps,

@@ -19,6 +19,9 @@ STATUS_NAMES = {0: "OGS_OK", 1: "OGS_EINVAL", 2: "OGS_ENOMEM", 3: "OGS_EDEVICE",
 
 SETUP_VERBOSE = 1
 SETUP_HOST_ONLY = 2
+SETUP_DEVICE_MAPS = 4
+SETUP_HOST_MAPS = 8
+DEVICE_MAPS_MIN_N = 65536
 
 # every symbol include/ogs_c.h declares: (name, restype, argtypes)
 _vp, _i, _i64, _u = C.c_void_p, C.c_int, C.c_int64, C.c_uint
@@ -37,6 +40,10 @@ SIGNATURES = {
     "ogs_get_counts": (_i, [_vp, _vp]),
     "ogs_get_maps": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "ogs_get_layout_stats": (_i, [_vp, _vp]),
+    "ogs_gslib_setup": (_i, [C.POINTER(_vp), _vp, _i64, _u]),
+    "ogs_gslib_gs": (_i, [_vp, _vp, _i, _i, _i, _vp]),
+    "ogs_gslib_gs_vec": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),
+    "ogs_gslib_gs_many": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),
     "ogs_batch_create": (_i, [C.POINTER(_vp), _i, _vp, _i, _u]),
     "ogs_batch_set_fields": (_i, [_vp, _vp, _vp]),
     "ogs_batch_gather_scatter": (_i, [_vp, _vp]),
@@ -67,7 +74,7 @@ class OgsCounts(C.Structure):
 class OgsLayoutStats(C.Structure):
     _fields_ = [("rows_by_degree", C.c_int64 * 9), ("nnz_general", C.c_int64),
                 ("ntiles", C.c_int64), ("device_bytes", C.c_int64), ("nphases", C.c_int64),
-                ("phases", (C.c_int64 * 4) * 8)]
+                ("phases", (C.c_int64 * 4) * 32)]
 
 
 class OgsBatchEntry(C.Structure):

@@ -28,12 +28,12 @@ constexpr int kBatchSmem = 2048;
 
 template <typename T, int D>
 __device__ __forceinline__ void fold_store_rt(int op, const WarpState& s, T* dst, int64_t stride, int K, int k,
-                                              bool gmask, bool smask, int lane, const T (&V)[kWarpSlots]) {
+                                              bool gmask, int smode, int lane, const T (&V)[kWarpSlots]) {
   switch (op) {
-    case OGS_ADD: warp_fold_store<T, OGS_ADD, kModeGS, D>(s, dst, nullptr, stride, K, k, gmask, smask, lane, V); break;
-    case OGS_MUL: warp_fold_store<T, OGS_MUL, kModeGS, D>(s, dst, nullptr, stride, K, k, gmask, smask, lane, V); break;
-    case OGS_MAX: warp_fold_store<T, OGS_MAX, kModeGS, D>(s, dst, nullptr, stride, K, k, gmask, smask, lane, V); break;
-    default: warp_fold_store<T, OGS_MIN, kModeGS, D>(s, dst, nullptr, stride, K, k, gmask, smask, lane, V); break;
+    case OGS_ADD: warp_fold_store<T, OGS_ADD, kModeGS, D>(s, dst, nullptr, stride, K, k, gmask, smode, false, lane, V); break;
+    case OGS_MUL: warp_fold_store<T, OGS_MUL, kModeGS, D>(s, dst, nullptr, stride, K, k, gmask, smode, false, lane, V); break;
+    case OGS_MAX: warp_fold_store<T, OGS_MAX, kModeGS, D>(s, dst, nullptr, stride, K, k, gmask, smode, false, lane, V); break;
+    default: warp_fold_store<T, OGS_MIN, kModeGS, D>(s, dst, nullptr, stride, K, k, gmask, smode, false, lane, V); break;
   }
 }
 
@@ -121,7 +121,8 @@ __global__ void __launch_bounds__(kBlock, OGS_BATCH_MINB) ogs_batch_kernel(const
   for (;;) {
     const bool more = i + W < nitems;
     const int K = cur.K, k = cur.k, d = cur.bucket_count >> 16;
-    const bool gmask = (cur.flags >> 4) & 1, smask = (cur.flags >> 5) & 1;
+    const bool gmask = (cur.flags >> 4) & 1;
+    const int smode = (cur.flags >> 5) & 1;
     T* base = static_cast<T*>(cur.v) + k;
     T V[kWarpSlots];
 #define OGS_B_VALS(D) warp_load_vals<T, kModeGS, D>(scur, base, nullptr, K, K, k, gmask, lane, V)
@@ -133,7 +134,7 @@ __global__ void __launch_bounds__(kBlock, OGS_BATCH_MINB) ogs_batch_kernel(const
       batch_load_state(nxt, lane, snxt);
       if (i + 2 * W < nitems) batch_item(E, st, n, i + 2 * W, nn);
     }
-#define OGS_B_FOLD(D) fold_store_rt<T, D>(cur.flags & 15, scur, base, K, K, k, gmask, smask, lane, V)
+#define OGS_B_FOLD(D) fold_store_rt<T, D>(cur.flags & 15, scur, base, K, K, k, gmask, smode, lane, V)
     OGS_DEGREE_SWITCH(d, OGS_B_FOLD)
 #undef OGS_B_FOLD
     if (!more) break;

@@ -31,6 +31,7 @@ size_t type_size(int type) { return (type == OGS_DOUBLE || type == OGS_INT64) ? 
 ogs_status check_common(ogs_handle h, int k, int type, int trans, const char* fn) {
   if (!h) return set_error(OGS_EINVAL, std::string(fn) + ": handle is NULL");
   if (h->host_only) return set_error(OGS_EINVAL, std::string(fn) + ": handle was set up host-only");
+  if (h->gslib) return set_error(OGS_EINVAL, std::string(fn) + ": handle was made by ogs_gslib_setup");
   if (k < 1) return set_error(OGS_EINVAL, std::string(fn) + ": k must be >= 1");
   if (type < OGS_FLOAT || type > OGS_INT64) return set_error(OGS_EINVAL, std::string(fn) + ": unknown type");
   if (trans < OGS_SYM || trans > OGS_TRANS) return set_error(OGS_EINVAL, std::string(fn) + ": unknown transpose");
@@ -108,20 +109,27 @@ ogs_status cuda_status(cudaError_t e, const char* fn, const char* what) {
   return set_error(OGS_EDEVICE, std::string(fn) + ": " + what + ": " + cudaGetErrorString(e));
 }
 
-// Copy streams and events of the host-buffer pipeline, made on first use.
+// Copy streams, capture stream and events of the host-buffer pipeline, made
+// on first use.
 ogs_status ensure_pipeline(ogs_handle_s* h, const char* fn) {
-  const size_t need = 1 + 2 * h->lay.phases.size();
+  const size_t need = 3 + 2 * h->lay.phases.size();
   if (h->copy_in && h->events.size() >= need) return OGS_OK;
   ogs_status s;
   if (!h->copy_in) {
-    cudaStream_t a = nullptr, b = nullptr;
+    cudaStream_t a = nullptr, b = nullptr, c = nullptr;
     if ((s = cuda_status(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking), fn, "stream")) != OGS_OK) return s;
     if ((s = cuda_status(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking), fn, "stream")) != OGS_OK) {
       cudaStreamDestroy(a);
       return s;
     }
+    if ((s = cuda_status(cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking), fn, "stream")) != OGS_OK) {
+      cudaStreamDestroy(a);
+      cudaStreamDestroy(b);
+      return s;
+    }
     h->copy_in = a;
     h->copy_out = b;
+    h->capture = c;
   }
   while (h->events.size() < need) {
     cudaEvent_t e = nullptr;
@@ -129,6 +137,80 @@ ogs_status ensure_pipeline(ogs_handle_s* h, const char* fn) {
     h->events.push_back(e);
   }
   return OGS_OK;
+}
+
+// The same pipeline captured once per (host buffer, k, type, op, transpose)
+// into a CUDA graph and replayed on `st`, so a repeated call costs one graph
+// launch (built when OGS_HOST_GRAPH is set).
+ogs_status host_pipeline_graph(ogs_handle_s* h, void* v, int k, int type, int op, int trans, const FieldArgs& f,
+                               const Pattern& pat, size_t node_bytes, cudaStream_t st, const char* fn) {
+  ogs_status s;
+  const size_t P = h->lay.phases.size();
+  ogs_handle_s::HostGraph* hit = nullptr;
+  for (auto& g : h->host_graphs)
+    if (g.host == v && g.k == k && g.type == type && g.op == op && g.trans == trans) hit = &g;
+  if (!hit) {
+    cudaStream_t cap = static_cast<cudaStream_t>(h->capture);
+    cudaStream_t sin = static_cast<cudaStream_t>(h->copy_in);
+    cudaStream_t sout = static_cast<cudaStream_t>(h->copy_out);
+    auto ev = [&](size_t i) { return static_cast<cudaEvent_t>(h->events[i]); };
+    char* dv = static_cast<char*>(h->stage);
+    char* hv = static_cast<char*>(v);
+    const std::vector<Phase>& ph = h->lay.phases;
+    if ((s = cuda_status(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), fn, "capture")) != OGS_OK)
+      return s;
+    cudaError_t ce = cudaEventRecord(ev(0), cap);
+    if (!ce) ce = cudaStreamWaitEvent(sin, ev(0), 0);
+    if (!ce) ce = cudaStreamWaitEvent(sout, ev(0), 0);
+    for (size_t p = 0; !ce && p < P; ++p) {
+      const size_t off = static_cast<size_t>(ph[p].h0) * node_bytes;
+      const size_t len = static_cast<size_t>(ph[p].h1 - ph[p].h0) * node_bytes;
+      if (len) ce = cudaMemcpyAsync(dv + off, hv + off, len, cudaMemcpyHostToDevice, sin);
+      if (!ce) ce = cudaEventRecord(ev(1 + 2 * p), sin);
+    }
+    ogs_status ls = OGS_OK;
+    for (size_t p = 0; !ce && ls == OGS_OK && p < P; ++p) {
+      ce = cudaStreamWaitEvent(cap, ev(1 + 2 * p), 0);
+      if (!ce) ls = launch_maps(phase_maps(h->dmaps, ph[p]), f, kModeGS, op, pat, type, cap, fn);
+      if (!ce && ls == OGS_OK) ce = cudaEventRecord(ev(2 + 2 * p), cap);
+    }
+    for (size_t p = 0; !ce && ls == OGS_OK && p < P; ++p) {
+      const size_t off = static_cast<size_t>(ph[p].d0) * node_bytes;
+      const size_t len = static_cast<size_t>(ph[p].d1 - ph[p].d0) * node_bytes;
+      if (!len) continue;
+      ce = cudaStreamWaitEvent(sout, ev(2 + 2 * p), 0);
+      if (!ce) ce = cudaMemcpyAsync(hv + off, dv + off, len, cudaMemcpyDeviceToHost, sout);
+    }
+    // join the copy streams back into the capture stream
+    if (!ce && ls == OGS_OK) ce = cudaEventRecord(ev(1 + 2 * P), sin);
+    if (!ce && ls == OGS_OK) ce = cudaEventRecord(ev(2 + 2 * P), sout);
+    if (!ce && ls == OGS_OK) ce = cudaStreamWaitEvent(cap, ev(1 + 2 * P), 0);
+    if (!ce && ls == OGS_OK) ce = cudaStreamWaitEvent(cap, ev(2 + 2 * P), 0);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(cap, &graph);
+    if (ls != OGS_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return ls;
+    }
+    if (ce || ee) {
+      if (graph) cudaGraphDestroy(graph);
+      cudaGetLastError();
+      return cuda_status(ce ? ce : ee, fn, "capture of the host pipeline");
+    }
+    cudaGraphExec_t exec = nullptr;
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if ((s = cuda_status(ce, fn, "instantiate")) != OGS_OK) return s;
+    if (h->host_graphs.size() >= 4) {  // keep the four most recent
+      cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(h->host_graphs.back().exec));
+      h->host_graphs.pop_back();
+    }
+    h->host_graphs.insert(h->host_graphs.begin(), ogs_handle_s::HostGraph{v, k, type, op, trans, exec});
+    hit = &h->host_graphs.front();
+  }
+  if ((s = cuda_status(cudaGraphLaunch(static_cast<cudaGraphExec_t>(hit->exec), st), fn, "graph launch")) != OGS_OK)
+    return s;
+  return cuda_status(cudaStreamSynchronize(st), fn, "synchronize");
 }
 
 }  // namespace
@@ -148,11 +230,19 @@ ogs_status ogs_setup_ex(ogs_handle* out, int64_t N, int64_t* ids, int kind, int 
   const auto t0 = std::chrono::steady_clock::now();
   ogs_handle_s* h = new (std::nothrow) ogs_handle_s();
   if (!h) return set_error(OGS_ENOMEM, "ogs_setup: out of host memory");
+  const bool host_only = (flags & OGS_SETUP_HOST_ONLY) != 0;
+  if ((flags & OGS_SETUP_DEVICE_MAPS) && (host_only || (flags & OGS_SETUP_HOST_MAPS))) {
+    delete h;
+    return set_error(OGS_EINVAL, "ogs_setup: OGS_SETUP_DEVICE_MAPS excludes HOST_ONLY and HOST_MAPS");
+  }
+  const bool device_maps =
+      (flags & OGS_SETUP_DEVICE_MAPS) ||
+      (!host_only && !(flags & OGS_SETUP_HOST_MAPS) && N >= OGS_DEVICE_MAPS_MIN_N);
   try {
-    ogs_status s = build_host_maps(h, N, ids, kind, unique);
+    ogs_status s = device_maps ? build_device_maps(h, N, ids, kind, unique) : build_host_maps(h, N, ids, kind, unique);
     if (s != OGS_OK) { delete h; return s; }
     build_layout(h);
-    h->host_only = (flags & OGS_SETUP_HOST_ONLY) != 0;
+    h->host_only = host_only;
     if (!h->host_only) {
       s = upload_layout(h);
       if (s != OGS_OK) { release_device(h); delete h; return s; }
@@ -271,7 +361,13 @@ ogs_status ogs_gather_scatter_host(ogs_handle h, void* v, int k, int type, int o
   f.v = h->stage;
   f.K = k;
   const Pattern pat = pattern_for(h, kModeGS, trans);
-  if (OGS_KERNEL != 0 || h->lay.phases.size() < 2) {
+  // The pipelined, graph-captured path needs page-locked host memory (copies
+  // from pageable memory cannot be captured and are staged by the driver
+  // anyway); pageable buffers take one copy in, the kernels, one copy out.
+  cudaPointerAttributes attr{};
+  const bool pinned = cudaPointerGetAttributes(&attr, v) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+  cudaGetLastError();
+  if (OGS_KERNEL != 0 || h->lay.phases.size() < 2 || !pinned) {
     if ((s = cuda_status(cudaMemcpyAsync(h->stage, v, bytes, cudaMemcpyHostToDevice, st), fn, "copy in")) != OGS_OK)
       return s;
     if ((s = launch(h, f, kModeGS, op, pat, type, stream, fn)) != OGS_OK) return s;
@@ -283,6 +379,7 @@ ogs_status ogs_gather_scatter_host(ogs_handle h, void* v, int k, int type, int o
   // Pipelined: chunk p goes in on copy_in while phase p-1 runs on `stream`
   // and the nodes that phase p-2 finished go out on copy_out.
   if ((s = ensure_pipeline(h, fn)) != OGS_OK) return s;
+  if (OGS_HOST_GRAPH) return host_pipeline_graph(h, v, k, type, op, trans, f, pat, node_bytes, st, fn);
   cudaStream_t sin = static_cast<cudaStream_t>(h->copy_in);
   cudaStream_t sout = static_cast<cudaStream_t>(h->copy_out);
   auto ev = [&](size_t i) { return static_cast<cudaEvent_t>(h->events[i]); };
@@ -421,7 +518,7 @@ ogs_status ogs_get_layout_stats(ogs_handle h, ogs_layout_stats* out) {
   out->ntiles = static_cast<int64_t>(h->lay.tiles.size());
   out->device_bytes = static_cast<int64_t>(h->arena_bytes);
   out->nphases = static_cast<int64_t>(h->lay.phases.size());
-  for (size_t p = 0; p < h->lay.phases.size() && p < 8; ++p) {
+  for (size_t p = 0; p < h->lay.phases.size() && p < 32; ++p) {
     const Phase& q = h->lay.phases[p];
     out->phases[p][0] = q.lo;
     out->phases[p][1] = q.hi;

@@ -28,6 +28,15 @@ constexpr int kTileNnz = 2048;
 constexpr int kEntriesPerThread = kTileNnz / kBlock;
 // General-bucket tiles hold at most one row per thread.
 constexpr int kGeneralRowsPerTile = kBlock;
+// Slices of the host-buffer pipeline (ogs_gather_scatter_host) and whether
+// the pipeline is captured into a CUDA graph and replayed on later calls with
+// the same host buffer.
+#ifndef OGS_HOST_PHASES
+#define OGS_HOST_PHASES 8
+#endif
+#ifndef OGS_HOST_GRAPH
+#define OGS_HOST_GRAPH 0
+#endif
 // Separate arrays handled by one launch of the *_many entry points.
 constexpr int kMaxMany = 16;
 // Member entries per lane of a warp tile (ogs_warp.cuh): lane l owns
@@ -126,8 +135,11 @@ struct DevMaps {
 // Which members take part, per ogsOperator.cpp:60-97, 206-238, 311-360.
 struct Pattern {
   int32_t gather_n;   // fold only members of the N map
-  int32_t scatter_n;  // write only members of the N map
+  int32_t scatter_n;  // 1: write only members of the N map; 2: those, or member 0
+                      //    when the row has none (gslib transpose 1)
   int32_t limit_n;    // process rows < NrowsN only
+  int32_t gslib = 0;  // gslib rules: fold from the first member taking part,
+                      //    integer Max starting at INT_MIN (gs_defs.h:44-52)
 };
 
 enum Mode : int { kModeGS = 0, kModeGather = 1, kModeScatter = 2 };
@@ -180,6 +192,7 @@ struct ogs_handle_s {
   int32_t max_degree = 0;
   bool host_only = false;
   bool covers_all = false;  // every local node is in the T map (no zero ids)
+  bool gslib = false;       // maps in gslib's member order (ogs_gslib.cpp)
 
   std::vector<int32_t> rowStartsT, colIdsT, rowStartsN, colIdsN;  // N empty when Unsigned
   ogsgb::HostLayout lay;
@@ -193,13 +206,22 @@ struct ogs_handle_s {
   size_t stage_bytes = 0;
   void* copy_in = nullptr;   // cudaStream_t: host->device chunks of the host pipeline
   void* copy_out = nullptr;  // cudaStream_t: device->host chunks
-  std::vector<void*> events; // cudaEvent_t: [0] call start, then 2 per phase
+  void* capture = nullptr;   // cudaStream_t: the pipeline is captured on it
+  std::vector<void*> events; // cudaEvent_t: [0] start, 2 per phase, then 2 joins
+  struct HostGraph {         // captured host-buffer pipelines, most recent first
+    void* host;
+    int k, type, op, trans;
+    void* exec;              // cudaGraphExec_t
+  };
+  std::vector<HostGraph> host_graphs;
 };
 
 namespace ogsgb {
 
 // Host setup (ogs_setup.cpp).
 ogs_status build_host_maps(ogs_handle_s* h, int64_t N, int64_t* ids, int kind, int unique);
+// The same maps built on the current device (ogs_dsetup.cu).
+ogs_status build_device_maps(ogs_handle_s* h, int64_t N, int64_t* ids, int kind, int unique);
 void build_layout(ogs_handle_s* h);
 ogs_status upload_layout(ogs_handle_s* h);
 void release_device(ogs_handle_s* h);

@@ -65,6 +65,15 @@ __device__ __forceinline__ void op_apply(T& a, const T b) {
   }
 }
 
+// gslib's identities (3rdParty/gslib/src/gs_defs.h:44-52): as ogs, except
+// integer Max, which starts from INT_MIN / LLONG_MIN.
+template <typename T, int OP>
+__device__ __forceinline__ T op_init_gs() {
+  if constexpr (OP == OGS_MAX && std::is_same<T, int32_t>::value) return INT32_MIN;
+  else if constexpr (OP == OGS_MAX && std::is_same<T, int64_t>::value) return INT64_MIN;
+  else return op_init<T, OP>();
+}
+
 // Address of component k of node 0; node c lives at base[c * stride].
 template <typename T>
 __device__ __forceinline__ T* field_base(const FieldArgs& f, int k) {
@@ -172,6 +181,15 @@ __device__ __forceinline__ void run_general(const DevGeneral& g, const Tile& t, 
     T a;
     if (MODE == kModeScatter) {
       a = static_cast<const T*>(f.gv)[r * K + k];
+    } else if (pat.gslib) {
+      // gslib: fold from the first member taking part (gs_local.c:58-72)
+      const T* src = field_base<T>(f, k);
+      if (g1 > g0) {
+        a = src[static_cast<int64_t>(gc[g0]) * stride];
+        for (int32_t q = g0 + 1; q < g1; ++q) op_apply<T, OP>(a, src[static_cast<int64_t>(gc[q]) * stride]);
+      } else {
+        a = op_init_gs<T, OP>();
+      }
     } else {
       const T* src = field_base<T>(f, k);
       a = op_init<T, OP>();
@@ -181,7 +199,11 @@ __device__ __forceinline__ void run_general(const DevGeneral& g, const Tile& t, 
       static_cast<T*>(f.gv)[r * K + k] = a;
     } else {
       T* dst = field_base<T>(f, k);
-      for (int32_t q = s0; q < s1; ++q) dst[static_cast<int64_t>(sc[q]) * stride] = a;
+      if (pat.scatter_n == 2 && g.startsN[i + 1] == g.startsN[i]) {
+        dst[static_cast<int64_t>(g.colsT[g.startsT[i]]) * stride] = a;  // no unflagged member: the primary only
+      } else {
+        for (int32_t q = s0; q < s1; ++q) dst[static_cast<int64_t>(sc[q]) * stride] = a;
+      }
     }
   }
 }

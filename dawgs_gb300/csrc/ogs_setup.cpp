@@ -292,7 +292,7 @@ void build_layout(ogs_handle_s* h) {
   }
   L.tiles.insert(L.tiles.end(), L.gtiles.begin(), L.gtiles.end());
   std::stable_sort(L.tiles.begin(), L.tiles.end(), by_row);
-  build_phases(h, 8);
+  build_phases(h, OGS_HOST_PHASES);
 }
 
 void build_phases(ogs_handle_s* h, int max_phases) {
@@ -377,6 +377,10 @@ DevMaps phase_maps(const DevMaps& m, const Phase& p) {
 }
 
 void release_device(ogs_handle_s* h) {
+  for (auto& g : h->host_graphs) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(g.exec));
+  h->host_graphs.clear();
+  if (h->capture) cudaStreamDestroy(static_cast<cudaStream_t>(h->capture));
+  h->capture = nullptr;
   for (void* e : h->events) cudaEventDestroy(static_cast<cudaEvent_t>(e));
   h->events.clear();
   if (h->copy_in) cudaStreamDestroy(static_cast<cudaStream_t>(h->copy_in));

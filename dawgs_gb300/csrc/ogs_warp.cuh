@@ -96,9 +96,13 @@ __device__ __forceinline__ void warp_load_vals(const WarpState& s, const T* src,
   }
 }
 
+// smode: 0 write every member, 1 only N members, 2 N members or, in a row
+// without any, member 0 (gslib transpose 1).  gslib: fold from the first
+// member taking part instead of from the identity (gs_local.c:58-72).
 template <typename T, int OP, int MODE, int D>
 __device__ __forceinline__ void warp_fold_store(const WarpState& s, T* dst, T* gv, int64_t stride, int K, int k,
-                                                bool gmask, bool smask, int lane, const T (&V)[kWarpSlots]) {
+                                                bool gmask, int smode, bool gslib, int lane,
+                                                const T (&V)[kWarpSlots]) {
   constexpr int RPT = warp_rows_per_lane(D);
 #pragma unroll
   for (int j = 0; j < RPT; ++j) {
@@ -106,6 +110,12 @@ __device__ __forceinline__ void warp_fold_store(const WarpState& s, T* dst, T* g
       T a;
       if (MODE == kModeScatter) {
         a = V[j];
+      } else if (gslib) {
+        // members are stored unflagged first, so member 0 takes part whenever any does
+        a = (!gmask || (s.emask >> (j * D)) & 1u) ? V[j * D] : op_init_gs<T, OP>();
+#pragma unroll
+        for (int q = 1; q < D; ++q)
+          if (!gmask || ((s.emask >> (j * D + q)) & 1u)) op_apply<T, OP>(a, V[j * D + q]);
       } else {
         a = op_init<T, OP>();
 #pragma unroll
@@ -115,10 +125,12 @@ __device__ __forceinline__ void warp_fold_store(const WarpState& s, T* dst, T* g
       if (MODE == kModeGather) {
         gv[static_cast<int64_t>(s.R[j]) * K + k] = a;
       } else {
+        const uint32_t row_n = (s.emask >> (j * D)) & ((1u << D) - 1u);
 #pragma unroll
         for (int q = 0; q < D; ++q) {
           const bool in_n = (s.emask >> (j * D + q)) & 1u;
-          if (smask && !in_n) continue;
+          if (smode == 1 && !in_n) continue;
+          if (smode == 2 && !(row_n ? in_n : q == 0)) continue;
           // a member that took part in the fold still holds its value in V
           if (OGS_SILENT_STORE && MODE == kModeGS && (!gmask || in_n) && same_bits(a, V[j * D + q])) continue;
           dst[static_cast<int64_t>(s.I[j * D + q]) * stride] = a;
@@ -150,7 +162,9 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const D
   int64_t i = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + (threadIdx.x >> 5);
   if (i >= nitems) return;
   const bool use_mask = (pat.gather_n || pat.scatter_n) && m.signed_maps;
-  const bool gmask = pat.gather_n != 0, smask = pat.scatter_n != 0;
+  const bool gmask = pat.gather_n != 0;
+  const int smode = pat.scatter_n;
+  const bool gslib = pat.gslib != 0;
   const int64_t stride = K1 ? 1 : (f.is_many ? 1 : K);
 
   int tcur = static_cast<int>(i / K);
@@ -183,7 +197,7 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const D
 #undef OGS_LOAD_NXT
       if (i + 2 * W < nitems) nn = m.wtiles[(i + 2 * W) / K];
     }
-#define OGS_FOLD(D) warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, k, gmask, smask, lane, V)
+#define OGS_FOLD(D) warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, k, gmask, smode, gslib, lane, V)
     OGS_DEGREE_SWITCH(cur.bucket, OGS_FOLD)
 #undef OGS_FOLD
     if (!more) break;

@@ -119,7 +119,9 @@ class ogs_t:
 
     # ogs_t::Setup, include/ogs.hpp:221-228 / libs/ogs/ogsSetup.cpp:44-53
     def Setup(self, N, ids, comm=None, kind=Unsigned, method=Auto, unique=False,
-              verbose=False, platform=None, host_only=False):
+              verbose=False, platform=None, host_only=False, maps=None):
+        """maps: None (GPU for N >= 65536 unless host_only), "device" or "host"
+        -- where the N/T maps are built; the handle is the same either way."""
         self.Free()
         if not (isinstance(ids, np.ndarray) and ids.dtype == np.int64 and ids.flags.c_contiguous):
             raise OgsError(_lib.OGS_EINVAL, "ids must be a contiguous int64 numpy array")
@@ -127,6 +129,9 @@ class ogs_t:
             raise OgsError(_lib.OGS_EINVAL, "ids is shorter than N")
         h = C.c_void_p()
         flags = (_lib.SETUP_VERBOSE if verbose else 0) | (_lib.SETUP_HOST_ONLY if host_only else 0)
+        if maps not in (None, "device", "host"):
+            raise OgsError(_lib.OGS_EINVAL, "maps must be None, 'device' or 'host'")
+        flags |= {None: 0, "device": _lib.SETUP_DEVICE_MAPS, "host": _lib.SETUP_HOST_MAPS}[maps]
         check(lib().ogs_setup_ex(C.byref(h), int(N), ids.ctypes.data, int(kind), int(bool(unique)), flags))
         self._h = h
         c = OgsCounts()
@@ -334,6 +339,46 @@ class ogs_server_t:
         if getattr(self, "_s", None) is not None and _lib._lib is not None:
             lib().ogs_server_free(self._s)
         self._s = None
+
+    def __del__(self):
+        try:
+            self.Free()
+        except Exception:
+            pass
+
+
+class gslib_t:
+    """gslib-compatible gather-scatter on the GPU (gs_setup / gs / gs_vec /
+    gs_many of the gslib that dawgs vendors, single rank, unique=0).  Negative
+    ids are flagged; transpose 0 or 1 as in gslib."""
+
+    def __init__(self, ids: np.ndarray, host_only=False):
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        h = C.c_void_p()
+        check(lib().ogs_gslib_setup(C.byref(h), ids.ctypes.data, ids.size,
+                                    _lib.SETUP_HOST_ONLY if host_only else 0))
+        self._h = h
+        self.n = ids.size
+
+    def gs(self, u, op=Add, transpose=0, stream=None):
+        check(lib().ogs_gslib_gs(self._h, _ptr(u), int(_type_of(u)), int(op), int(transpose), _stream_of(stream)))
+        return u
+
+    def gs_vec(self, u, vn, op=Add, transpose=0, stream=None):
+        check(lib().ogs_gslib_gs_vec(self._h, _ptr(u), int(vn), int(_type_of(u)), int(op), int(transpose),
+                                     _stream_of(stream)))
+        return u
+
+    def gs_many(self, us, op=Add, transpose=0, stream=None):
+        arr = (C.c_void_p * len(us))(*[_ptr(x) for x in us])
+        check(lib().ogs_gslib_gs_many(self._h, arr, len(us), int(_type_of(us[0])), int(op), int(transpose),
+                                      _stream_of(stream)))
+        return us
+
+    def Free(self):
+        if getattr(self, "_h", None) is not None and _lib._lib is not None:
+            lib().ogs_free(self._h)
+        self._h = None
 
     def __del__(self):
         try:

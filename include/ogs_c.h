@@ -55,6 +55,12 @@ typedef enum { OGS_UNSIGNED = 0, OGS_SIGNED = 1, OGS_HALO = 2 } ogs_kind;
 /* setup flags for ogs_setup_ex */
 #define OGS_SETUP_VERBOSE   1u  /* print the reference's "ogs Setup Time" line */
 #define OGS_SETUP_HOST_ONLY 2u  /* build host maps only; no device memory, no ops */
+/* Where the N/T maps are built (the result is the same either way).  With
+ * neither flag, a handle that is not host-only of at least
+ * OGS_DEVICE_MAPS_MIN_N local nodes builds them on the GPU. */
+#define OGS_SETUP_DEVICE_MAPS 4u /* sort and scan on the GPU; not with HOST_ONLY */
+#define OGS_SETUP_HOST_MAPS   8u /* hash-table pass on the host */
+#define OGS_DEVICE_MAPS_MIN_N 65536
 
 typedef struct {
   int64_t N;              /* local nodes (ogsBase_t::N) */
@@ -73,8 +79,8 @@ typedef struct {
   int64_t nnz_general;       /* entries in rows above degree 8 */
   int64_t ntiles;            /* work tiles in one launch over the whole map */
   int64_t device_bytes;      /* device memory held by the handle's maps */
-  int64_t nphases;           /* slices of the host-buffer pipeline (at most 8) */
-  int64_t phases[8][4];      /* per slice: lowest and highest node it touches, end of its
+  int64_t nphases;           /* slices of the host-buffer pipeline (at most 32) */
+  int64_t phases[32][4];     /* per slice: lowest and highest node it touches, end of its
                                 host->device chunk, end of the nodes final after it */
 } ogs_layout_stats;
 
@@ -148,6 +154,22 @@ ogs_status ogs_get_maps(ogs_handle h, int32_t *rowStartsT, int32_t *colIdsT,
                         int32_t *rowStartsN, int32_t *colIdsN);
 /* Degree buckets and tiles the kernels run over (no reference counterpart). */
 ogs_status ogs_get_layout_stats(ogs_handle h, ogs_layout_stats *out);
+
+/* ---- gslib-compatible entry points ----
+ * gslib (3rdParty/gslib of the reference) is the gather-scatter that dawgs
+ * checks ogs against (dawgsGS.cpp:34-105).  These calls give its single-rank
+ * results on the GPU, bit for bit: gs_setup(id, n, comm, unique=0, method,
+ * verbose) (gs.c:1441), gs(u, dom, op, transpose) (gs.c:1266), gs_vec
+ * (gs.c:1322) and gs_many (gs.c:1354).  Negative ids are flagged; transpose 0
+ * folds unflagged members and sends the result to every member, transpose 1
+ * folds all and writes the unflagged ones; see ogs_gslib.cpp for the rules.
+ * dom uses ogs_type codes; ops add, mul, max, min (no bpr).  Free with
+ * ogs_free.  A gslib handle is not accepted by the ogs_* operations. */
+ogs_status ogs_gslib_setup(ogs_handle *out, const int64_t *ids, int64_t n, unsigned flags);
+ogs_status ogs_gslib_gs(ogs_handle h, void *d_u, int dom, int op, int transpose, void *stream);
+ogs_status ogs_gslib_gs_vec(ogs_handle h, void *d_u, int vn, int dom, int op, int transpose, void *stream);
+ogs_status ogs_gslib_gs_many(ogs_handle h, void *const *d_us, int vn, int dom, int op, int transpose,
+                             void *stream);
 
 /* ---- Batched gather-scatter: many meshes in one persistent launch ----
  * No reference counterpart (dawgs calls ogs_t::GatherScatter once per mesh,

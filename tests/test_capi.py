@@ -56,6 +56,10 @@ def test_rejects_invalid_setups(built_lib):
     assert built_lib.ogs_setup_ex(C.byref(h), 5, None, 0, 0, _lib.SETUP_HOST_ONLY) == _lib.OGS_EINVAL
     assert built_lib.ogs_setup_ex(None, 5, ids.ctypes.data, 0, 0, _lib.SETUP_HOST_ONLY) == _lib.OGS_EINVAL
     assert built_lib.ogs_setup(C.byref(h), 10, ids.ctypes.data, 0, 9, 0, 0) == _lib.OGS_EINVAL  # method
+    # maps on the GPU exclude a host-only handle and the host-maps flag
+    for flags in (_lib.SETUP_DEVICE_MAPS | _lib.SETUP_HOST_ONLY, _lib.SETUP_DEVICE_MAPS | _lib.SETUP_HOST_MAPS):
+        assert built_lib.ogs_setup_ex(C.byref(h), 10, ids.ctypes.data, 0, 0, flags) == _lib.OGS_EINVAL
+    assert b"DEVICE_MAPS" in built_lib.ogs_last_error_string()
 
 
 def test_host_only_handle_rejects_ops(built_lib):

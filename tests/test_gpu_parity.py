@@ -173,3 +173,31 @@ def test_side_stream_and_repeatability(cuda, oracle_mod):
         outs.append(d.cpu().numpy())
     for o in outs:
         assert same_bits(o, want)
+
+
+def test_host_pipeline_graph_replay_and_cache(cuda, oracle_mod):
+    """The host-buffer call captures its copy/compute pipeline once per buffer
+    and parameters and replays it: repeated calls on one buffer, calls that
+    rotate through more buffers than the cache keeps, and changing k or op all
+    give the oracle's result."""
+    ids = mesh.box_ids(12, 10, 9, 4)  # enough tiles for a multi-slice pipeline
+    g = ogs.ogs_t().Setup(ids.size, ids.copy())
+    assert len(g.layout_stats()["phases"]) > 1
+    ref = oracle_mod.OracleOgs(ids.copy(), "unsigned")
+    buf = torch.empty(2 * ids.size, dtype=torch.float64).pin_memory()
+    for rep in range(3):
+        v = values(ids.size, np.float64, "add", seed=60 + rep)
+        buf[: ids.size].copy_(torch.from_numpy(v))
+        g.GatherScatter(buf[: ids.size], 1, ogs.Add, ogs.Sym)
+        assert same_bits(buf[: ids.size].numpy(), ref.gather_scatter(v.copy(), 1, "add", "sym"))
+    v2 = values(2 * ids.size, np.float64, "max", seed=70)
+    buf.copy_(torch.from_numpy(v2))
+    g.GatherScatter(buf, 2, ogs.Max, ogs.Sym)
+    assert same_bits(buf.numpy(), ref.gather_scatter(v2.copy(), 2, "max", "sym"))
+    bufs = [torch.from_numpy(values(ids.size, np.float64, "add", seed=80 + j)).pin_memory() for j in range(6)]
+    for _ in range(2):
+        for j, b in enumerate(bufs):
+            v = values(ids.size, np.float64, "add", seed=80 + j)
+            b.copy_(torch.from_numpy(v))
+            g.GatherScatter(b, 1, ogs.Add, ogs.Sym)
+            assert same_bits(b.numpy(), ref.gather_scatter(v.copy(), 1, "add", "sym"))
