@@ -1,0 +1,248 @@
+// ogs_async.cuh -- the warp pipeline with its value gathers staged through
+// shared memory by cp.async.
+//
+// Same work items, arithmetic and stores as ogs_warp_kernel (ogs_warp.cuh;
+// the reference fold is ogsOperator.cpp:60-97, 206-238, 311-360).  What
+// changes is how many loads a warp keeps in flight.  The register pipeline
+// holds one item's values and the next item's column ids; its registers cap
+// it there, and the kernel is latency-bound (ncu: DRAM well under half busy,
+// long-scoreboard stalls first).  Here the value gathers of an item are
+// cp.async copies into a per-warp ring of shared memory, which hold no
+// registers while in flight, so each warp keeps two items' values and a
+// third item's column ids in flight:
+//
+//   iteration for item i:  issue gathers of item i+W into stage (s+1) % 3
+//                          issue column-id loads of item i+2W (registers)
+//                          wait for the gathers of item i (stage s)
+//                          fold item i from shared memory, store
+//
+// Every lane gathers and later folds its own entries only, so no barrier of
+// any kind is needed: cp.async.wait_group makes a thread's own completed
+// copies visible to it.  With three stages, the stage an iteration refills
+// was read two iterations earlier.
+#pragma once
+
+#include <cstdint>
+
+#include "ogs_warp.cuh"
+
+#ifndef OGS_ASYNC
+#define OGS_ASYNC 1
+#endif
+
+namespace ogsgb {
+
+constexpr int kAsyncStages = 3;
+
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem) {
+  const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+  if (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Entry e of this lane lives at stage[e * 32 + lane].
+template <typename T, int MODE, int D>
+__device__ __forceinline__ void async_issue_vals(const WarpState& s, const T* src, const T* gv, int64_t stride, int K,
+                                                 int k, bool gmask, int lane, T* stage) {
+  constexpr int RPT = warp_rows_per_lane(D);
+#pragma unroll
+  for (int j = 0; j < RPT; ++j) {
+    if (j * 32 + lane < s.cnt) {
+      if (MODE == kModeScatter) {
+        cp_async_elem(stage + j * 32 + lane, gv + static_cast<int64_t>(s.R[j]) * K + k);
+      } else {
+#pragma unroll
+        for (int q = 0; q < D; ++q)
+          if (!gmask || ((s.emask >> (j * D + q)) & 1u))
+            cp_async_elem(stage + (j * D + q) * 32 + lane, src + static_cast<int64_t>(s.I[j * D + q]) * stride);
+      }
+    }
+  }
+}
+
+template <typename T, int MODE, int D>
+__device__ __forceinline__ void async_read_vals(const WarpState& s, bool gmask, int lane, const T* stage,
+                                                T (&V)[kWarpSlots]) {
+  constexpr int RPT = warp_rows_per_lane(D);
+#pragma unroll
+  for (int j = 0; j < RPT; ++j) {
+    if (j * 32 + lane < s.cnt) {
+      if (MODE == kModeScatter) {
+        V[j] = stage[j * 32 + lane];
+      } else {
+#pragma unroll
+        for (int q = 0; q < D; ++q)
+          if (!gmask || ((s.emask >> (j * D + q)) & 1u)) V[j * D + q] = stage[(j * D + q) * 32 + lane];
+      }
+    }
+  }
+}
+
+template <typename T>
+constexpr size_t async_smem_bytes() {
+  return static_cast<size_t>(kBlock / 32) * kAsyncStages * kWarpSlots * 32 * sizeof(T);
+}
+
+template <typename T, int OP, int MODE, int KL>
+__global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const DevMaps m, const FieldArgs f,
+                                                                          const Pattern pat) {
+  extern __shared__ __align__(16) unsigned char async_smem[];
+  const int lane = static_cast<int>(threadIdx.x) & 31;
+  const int warp = static_cast<int>(threadIdx.x) >> 5;
+  T* ring = reinterpret_cast<T*>(async_smem) + static_cast<size_t>(warp) * kAsyncStages * kWarpSlots * 32;
+  const int64_t W = static_cast<int64_t>(gridDim.x) * (kBlock / 32);
+  const int K = KL == kK1 ? 1 : f.K;
+  const int64_t nw = m.nwtiles;
+  const int64_t nitems = nw * K;
+  int64_t i = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + warp;
+  if (i >= nitems) return;
+  const bool use_mask = (pat.gather_n || pat.scatter_n) && m.signed_maps;
+  const bool gmask = pat.gather_n != 0;
+  const int smode = pat.scatter_n;
+  const bool gslib = pat.gslib != 0;
+  const int64_t stride = KL == kKInterleaved ? K : 1;
+  auto tile_of = [&](int64_t item) {
+    return static_cast<int>(KL == kKMany ? item % nw : (KL == kKInterleaved ? item / K : item));
+  };
+  auto comp_of = [&](int64_t item) {
+    return KL == kKMany ? static_cast<int>(item / nw) : (KL == kKInterleaved ? static_cast<int>(item % K) : 0);
+  };
+  T* gv = static_cast<T*>(f.gv);
+
+  // prologue: state and gathers of item i, state of item i+W, descriptor of i+2W
+  int tcur = tile_of(i);
+  Tile cur = m.wtiles[tcur];
+  WarpState scur, snxt;
+#define OGS_A_LOAD(D, TILE, TI, S) warp_load_state<MODE, D>(m.b[D], TILE, m.wemask, TI, use_mask, pat, lane, S)
+#define OGS_A_LOAD_CUR(D) OGS_A_LOAD(D, cur, tcur, scur)
+  OGS_DEGREE_SWITCH(cur.bucket, OGS_A_LOAD_CUR)
+#undef OGS_A_LOAD_CUR
+  {
+    const int k0 = comp_of(i);
+    const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, k0);
+#define OGS_A_ISSUE0(D) async_issue_vals<T, MODE, D>(scur, src, gv, stride, K, k0, gmask, lane, ring)
+    OGS_DEGREE_SWITCH(cur.bucket, OGS_A_ISSUE0)
+#undef OGS_A_ISSUE0
+  }
+  cp_async_commit();
+  Tile nxt{}, nn{};
+  int tnxt = 0;
+  if (i + W < nitems) {
+    tnxt = tile_of(i + W);
+    nxt = m.wtiles[tnxt];
+#define OGS_A_LOAD_NXT(D) OGS_A_LOAD(D, nxt, tnxt, snxt)
+    OGS_DEGREE_SWITCH(nxt.bucket, OGS_A_LOAD_NXT)
+#undef OGS_A_LOAD_NXT
+    if (i + 2 * W < nitems) nn = m.wtiles[tile_of(i + 2 * W)];
+  }
+
+  int stage = 0;
+  for (;;) {
+    const bool more1 = i + W < nitems;
+    const bool more2 = i + 2 * W < nitems;
+    const int nstage = stage == kAsyncStages - 1 ? 0 : stage + 1;
+    if (more1) {
+      const int k1 = comp_of(i + W);
+      const T* src1 = (MODE == kModeScatter) ? nullptr : field_base<T>(f, k1);
+      T* st1 = ring + nstage * (kWarpSlots * 32);
+#define OGS_A_ISSUE1(D) async_issue_vals<T, MODE, D>(snxt, src1, gv, stride, K, k1, gmask, lane, st1)
+      OGS_DEGREE_SWITCH(nxt.bucket, OGS_A_ISSUE1)
+#undef OGS_A_ISSUE1
+    }
+    cp_async_commit();
+    WarpState snn;
+    Tile n3{};
+    int tnn = 0;
+    if (more2) {
+      tnn = tile_of(i + 2 * W);
+#define OGS_A_LOAD_NN(D) OGS_A_LOAD(D, nn, tnn, snn)
+      OGS_DEGREE_SWITCH(nn.bucket, OGS_A_LOAD_NN)
+#undef OGS_A_LOAD_NN
+      if (i + 3 * W < nitems) n3 = m.wtiles[tile_of(i + 3 * W)];
+    }
+    cp_async_wait<1>();  // the gathers of item i are in
+    {
+      const int k0 = comp_of(i);
+      T* dst = (MODE == kModeGather) ? nullptr : field_base<T>(f, k0);
+      const T* st0 = ring + stage * (kWarpSlots * 32);
+      T V[kWarpSlots];
+#define OGS_A_FOLD(D)                                                                            \
+  do {                                                                                           \
+    async_read_vals<T, MODE, D>(scur, gmask, lane, st0, V);                                      \
+    warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, k0, gmask, smode, gslib, lane, V); \
+  } while (0)
+      OGS_DEGREE_SWITCH(cur.bucket, OGS_A_FOLD)
+#undef OGS_A_FOLD
+    }
+    if (!more1) break;
+    i += W;
+    stage = nstage;
+    cur = nxt;
+    scur = snxt;
+    tcur = tnxt;
+    nxt = nn;
+    snxt = snn;
+    tnxt = tnn;
+    nn = n3;
+  }
+  cp_async_wait<0>();
+#undef OGS_A_LOAD
+}
+
+template <typename T, int OP, int MODE, int KL>
+inline int async_grid(int64_t nitems) {
+  static int cached_dev = -1, cached = 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != cached_dev) {
+    int bps = 0, sms = 0;
+    // above 48 KB (more entries per lane) the dynamic shared memory must be opted into
+    if (async_smem_bytes<T>() > 48 * 1024)
+      cudaFuncSetAttribute(ogs_async_kernel<T, OP, MODE, KL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           static_cast<int>(async_smem_bytes<T>()));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_async_kernel<T, OP, MODE, KL>, kBlock,
+                                                  async_smem_bytes<T>());
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cached = (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1);
+    cached_dev = dev;
+  }
+  const int64_t need = (nitems + (kBlock / 32) - 1) / (kBlock / 32);
+  return static_cast<int>(need < cached ? need : cached);
+}
+
+template <typename T, int OP, int MODE, int KL>
+inline void launch_async_kl(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
+  const int grid = async_grid<T, OP, MODE, KL>(static_cast<int64_t>(m.nwtiles) * (KL == kK1 ? 1 : f.K));
+  ogs_async_kernel<T, OP, MODE, KL><<<grid, kBlock, async_smem_bytes<T>(), s>>>(m, f, pat);
+}
+
+// Exact-degree tiles on the async pipeline, general tiles on the direct kernel.
+template <typename T, int OP, int MODE>
+inline cudaError_t launch_async(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
+  if (m.nwtiles > 0) {
+    if (f.is_many) launch_async_kl<T, OP, MODE, kKMany>(m, f, pat, s);
+    else if (f.K == 1) launch_async_kl<T, OP, MODE, kK1>(m, f, pat, s);
+    else launch_async_kl<T, OP, MODE, kKInterleaved>(m, f, pat, s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (m.ngtiles > 0) {
+    DevMaps g = m;
+    g.tiles = m.gtiles;
+    g.ntiles = m.ngtiles;
+    return launch_direct<T, OP, MODE>(g, f, pat, s);
+  }
+  return cudaSuccess;
+}
+
+}  // namespace ogsgb

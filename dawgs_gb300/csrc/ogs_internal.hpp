@@ -37,6 +37,12 @@ constexpr int kGeneralRowsPerTile = kBlock;
 #ifndef OGS_HOST_GRAPH
 #define OGS_HOST_GRAPH 0
 #endif
+// With 6 or more slices, the first and last two take 1/4 and 1/2 of the
+// others' share of tiles: the first copy in and the last copy out run with
+// nothing beside them, so they are kept short.
+#ifndef OGS_HOST_TAPER
+#define OGS_HOST_TAPER 1
+#endif
 // Separate arrays handled by one launch of the *_many entry points.
 constexpr int kMaxMany = 16;
 // Member entries per lane of a warp tile (ogs_warp.cuh): lane l owns

@@ -1,12 +1,13 @@
 // ogs_launch.cuh -- per-type launch dispatch shared by ogs_kern_*.cu.
 //
-// Exact-degree rows run on the warp-pipelined kernel (ogs_warp.cuh) for every
-// k and layout; rows above degree 8 on the direct CTA kernel
+// Exact-degree rows run on the warp pipeline with cp.async-staged gathers
+// (ogs_async.cuh; -DOGS_ASYNC=0: the register pipeline of ogs_warp.cuh) for
+// every k and layout; rows above degree 8 on the direct CTA kernel
 // (ogs_kernels.cuh).  Building with -DOGS_KERNEL=2 runs the direct CTA
 // kernel for every row instead (for comparisons).
 #pragma once
 
-#include "ogs_warp.cuh"
+#include "ogs_async.cuh"
 
 #ifndef OGS_KERNEL
 #define OGS_KERNEL 0
@@ -17,6 +18,7 @@ namespace ogsgb {
 template <typename T, int OP, int MODE>
 inline cudaError_t launch_mode(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
   if (OGS_KERNEL == 2) return launch_direct<T, OP, MODE>(m, f, pat, s);
+  if (OGS_ASYNC) return launch_async<T, OP, MODE>(m, f, pat, s);
   return launch_warp<T, OP, MODE>(m, f, pat, s);
 }
 

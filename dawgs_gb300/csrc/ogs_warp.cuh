@@ -5,7 +5,8 @@
 // 311-360).  The data movement is organised per warp, with no block-level
 // synchronisation at all:
 //
-//  * Work items are (warp tile, component k).  A warp tile holds 32 lanes x
+//  * Work items are warp tiles (and, for separate arrays, the array; see
+//    KLayout).  A warp tile holds 32 lanes x
 //    kWarpEntries member entries of one exact-degree bucket: lane l owns rows
 //    l, l+32, ... of the tile, each with its d members.  Tiles are ordered by
 //    first row; warp w of the grid takes items w, w+W, w+2W, ... so the grid
@@ -152,38 +153,54 @@ __device__ __forceinline__ void warp_fold_store(const WarpState& s, T* dst, T* g
     default: CALL(8); break;            \
   }
 
-template <typename T, int OP, int MODE, bool K1>
+// How the k components of a field map onto work items.
+enum KLayout : int {
+  kK1 = 0,          // k = 1: item = tile
+  kKInterleaved = 1,  // v[c + n*k], k > 1: item = (tile, component), tile-major,
+                      // so the k warps of one tile run side by side and share
+                      // the sectors of each node's k values.  (One item per
+                      // tile looping over the components was slower: 86 vs
+                      // 66 us for k = 3 on 3.5 M permuted nodes.)
+  kKMany = 2,       // k separate arrays: item = (array, tile), array-major, so
+                    // one array and the column ids stay resident in L2 while
+                    // the grid sweeps that array
+};
+
+template <typename T, int OP, int MODE, int KL>
 __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const DevMaps m, const FieldArgs f,
                                                                          const Pattern pat) {
   const int lane = static_cast<int>(threadIdx.x) & 31;
   const int64_t W = static_cast<int64_t>(gridDim.x) * (kBlock / 32);
-  const int K = K1 ? 1 : f.K;
-  const int64_t nitems = static_cast<int64_t>(m.nwtiles) * K;
+  const int K = KL == kK1 ? 1 : f.K;
+  const int64_t nw = m.nwtiles;
+  const int64_t nitems = nw * K;
   int64_t i = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + (threadIdx.x >> 5);
   if (i >= nitems) return;
   const bool use_mask = (pat.gather_n || pat.scatter_n) && m.signed_maps;
   const bool gmask = pat.gather_n != 0;
   const int smode = pat.scatter_n;
   const bool gslib = pat.gslib != 0;
-  const int64_t stride = K1 ? 1 : (f.is_many ? 1 : K);
+  const int64_t stride = KL == kKInterleaved ? K : 1;
+  auto tile_of = [&](int64_t item) {
+    return static_cast<int>(KL == kKMany ? item % nw : (KL == kKInterleaved ? item / K : item));
+  };
 
-  int tcur = static_cast<int>(i / K);
+  int tcur = tile_of(i);
   Tile cur = m.wtiles[tcur];
   WarpState scur;
 #define OGS_LOAD_CUR(D) warp_load_state<MODE, D>(m.b[D], cur, m.wemask, tcur, use_mask, pat, lane, scur)
   OGS_DEGREE_SWITCH(cur.bucket, OGS_LOAD_CUR)
 #undef OGS_LOAD_CUR
   Tile nxt{};
-  if (i + W < nitems) nxt = m.wtiles[(i + W) / K];
+  if (i + W < nitems) nxt = m.wtiles[tile_of(i + W)];
 
+  T* gv = static_cast<T*>(f.gv);
   for (;;) {
-    const int k = K1 ? 0 : static_cast<int>(i % K);
-
-    const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, k);
-    T* dst = (MODE == kModeGather) ? nullptr : field_base<T>(f, k);
-    T* gv = static_cast<T*>(f.gv);
+    const int k0 = KL == kKMany ? static_cast<int>(i / nw) : (KL == kKInterleaved ? static_cast<int>(i % K) : 0);
+    const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, k0);
+    T* dst = (MODE == kModeGather) ? nullptr : field_base<T>(f, k0);
     T V[kWarpSlots];
-#define OGS_VALS(D) warp_load_vals<T, MODE, D>(scur, src, gv, stride, K, k, gmask, lane, V)
+#define OGS_VALS(D) warp_load_vals<T, MODE, D>(scur, src, gv, stride, K, k0, gmask, lane, V)
     OGS_DEGREE_SWITCH(cur.bucket, OGS_VALS)
 #undef OGS_VALS
     const bool more = i + W < nitems;
@@ -191,13 +208,13 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const D
     Tile nn{};
     int tnxt = 0;
     if (more) {
-      tnxt = static_cast<int>((i + W) / K);
+      tnxt = tile_of(i + W);
 #define OGS_LOAD_NXT(D) warp_load_state<MODE, D>(m.b[D], nxt, m.wemask, tnxt, use_mask, pat, lane, snxt)
       OGS_DEGREE_SWITCH(nxt.bucket, OGS_LOAD_NXT)
 #undef OGS_LOAD_NXT
-      if (i + 2 * W < nitems) nn = m.wtiles[(i + 2 * W) / K];
+      if (i + 2 * W < nitems) nn = m.wtiles[tile_of(i + 2 * W)];
     }
-#define OGS_FOLD(D) warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, k, gmask, smode, gslib, lane, V)
+#define OGS_FOLD(D) warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, k0, gmask, smode, gslib, lane, V)
     OGS_DEGREE_SWITCH(cur.bucket, OGS_FOLD)
 #undef OGS_FOLD
     if (!more) break;
@@ -210,14 +227,14 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const D
 }
 
 // CTAs of the warp kernel resident per SM, once per instantiation and device.
-template <typename T, int OP, int MODE, bool K1>
+template <typename T, int OP, int MODE, int KL>
 inline int warp_grid(int64_t nitems) {
   static int cached_dev = -1, cached = 0;
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev != cached_dev) {
     int bps = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_warp_kernel<T, OP, MODE, K1>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_warp_kernel<T, OP, MODE, KL>, kBlock, 0);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cached = (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1);
     cached_dev = dev;
@@ -228,14 +245,16 @@ inline int warp_grid(int64_t nitems) {
 
 template <typename T, int OP, int MODE>
 inline cudaError_t launch_warp(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
-  const int64_t nitems = static_cast<int64_t>(m.nwtiles) * f.K;
-  if (nitems > 0) {
-    if (f.K == 1 && !f.is_many) {
-      const int grid = warp_grid<T, OP, MODE, true>(nitems);
-      ogs_warp_kernel<T, OP, MODE, true><<<grid, kBlock, 0, s>>>(m, f, pat);
+  if (m.nwtiles > 0) {
+    if (f.is_many) {
+      const int grid = warp_grid<T, OP, MODE, kKMany>(static_cast<int64_t>(m.nwtiles) * f.K);
+      ogs_warp_kernel<T, OP, MODE, kKMany><<<grid, kBlock, 0, s>>>(m, f, pat);
+    } else if (f.K == 1) {
+      const int grid = warp_grid<T, OP, MODE, kK1>(static_cast<int64_t>(m.nwtiles));
+      ogs_warp_kernel<T, OP, MODE, kK1><<<grid, kBlock, 0, s>>>(m, f, pat);
     } else {
-      const int grid = warp_grid<T, OP, MODE, false>(nitems);
-      ogs_warp_kernel<T, OP, MODE, false><<<grid, kBlock, 0, s>>>(m, f, pat);
+      const int grid = warp_grid<T, OP, MODE, kKInterleaved>(static_cast<int64_t>(m.nwtiles) * f.K);
+      ogs_warp_kernel<T, OP, MODE, kKInterleaved><<<grid, kBlock, 0, s>>>(m, f, pat);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
