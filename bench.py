@@ -62,7 +62,9 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-meshes", type=int, default=256)
     ap.add_argument("--no-served", action="store_true")
-    ap.add_argument("--served-requests", type=int, default=20000)
+    ap.add_argument("--served-requests", type=int, default=100000)
+    ap.add_argument("--sweep", action="store_true",
+                    help="print the results tables (one JSON line per case) instead of the bench line")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     return a
@@ -430,6 +432,18 @@ def run_ours(a):
     t_kernel, _, value = aggregate_over_ranks(sum(kt), g.NgatherGlobal * a.steps, dev)
     per_step = t_kernel / a.steps
 
+    # warm: back-to-back calls on one field, no flush and no restore, so the
+    # column ids and the field stay in L2 between calls (reported beside the
+    # cold headline, not instead of it)
+    wev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    work.copy_(pristine)
+    for _ in range(3):
+        step()
+    for e0, e1 in wev:
+        step(e0, e1)
+    torch.cuda.synchronize(dev)
+    warm_per_step = sum(e0.elapsed_time(e1) * 1e-3 for e0, e1 in wev) / a.steps
+
     # e2e through the C ABI host-buffer entry point, pinned host memory
     e2e = None
     if not a.no_e2e:
@@ -494,6 +508,8 @@ def run_ours(a):
                    "tiles": stats["ntiles"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profiled_traffic(),
+                     "warm": {"ms_per_step": warm_per_step * 1e3, "achieved": nbytes_alg / warm_per_step / 1e9,
+                              "frac": nbytes_alg / warm_per_step / 1e9 / peak},
                      "alg_bytes_per_launch": nbytes_alg, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"
                      if peak_src == "measured" else "fallback 6.8 TB/s"},
         "cpu_baseline": cpu,
@@ -513,10 +529,121 @@ def run_ours(a):
     return 0
 
 
+def run_sweep(a):
+    """The results tables: one JSON line per case, on cuda:0.
+
+    24^3 box, fp64 Add GatherScatter for p = 1..15; at p = 7 also fp32 Add,
+    int32/int64 Min/Max, Gather (Trans) and Scatter (NoTrans) on a Signed
+    unique handle; the 32x32x16 p=5 mesh with a seeded element permutation,
+    k = 1, k = 3 interleaved and k = 8 separate arrays, fp64/fp32 Add/Mul.
+    cold: the field restored and L2 flushed (write then read 2x L2) before
+    every timed call; warm (Add cases): back-to-back calls on one field."""
+    import ctypes as C
+    import torch
+    from dawgs_gb300 import _lib, mesh, ogs
+    L = _lib.lib()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    peak, _ = hbm_peak()
+    l2 = torch.cuda.get_device_properties(dev).L2_cache_size
+    flush = torch.empty(2 * l2 // 4 + 1, dtype=torch.float32, device=dev)
+    sink = torch.empty((), dtype=torch.float32, device=dev)
+    st = torch.cuda.current_stream(dev)
+    tcode = {torch.float64: 1, torch.float32: 0, torch.int32: 2, torch.int64: 3}
+    reps = max(a.steps, 5)
+
+    def timeit(fn, restore=None, cold=True):
+        ts = []
+        for i in range(reps + 3):
+            if restore is not None:
+                restore()
+            if cold:
+                flush.zero_()
+                torch.sum(flush, dim=0, out=sink)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            rc = fn()
+            e1.record(st)
+            torch.cuda.synchronize(dev)
+            if rc:
+                raise SystemExit(f"bench --sweep: status {rc}: {L.ogs_last_error_string().decode()}")
+            if i >= 3:
+                ts.append(e0.elapsed_time(e1) * 1e-3)
+        return float(np.median(ts))
+
+    def emit(case, g, k, t, ab, warm=None):
+        r = {"case": case, "local_dofs": int(g.N), "global_dofs": int(g.NgatherGlobal), "k": k,
+             "us_cold": t * 1e6, "dofs_per_s_cold": g.NgatherGlobal * k / t, "gbs_cold": ab / t / 1e9,
+             "frac_cold": ab / t / 1e9 / peak, "alg_bytes": int(ab)}
+        if warm is not None:
+            r.update(us_warm=warm * 1e6, frac_warm=ab / warm / 1e9 / peak)
+        print(json.dumps(r), flush=True)
+
+    def gs(case, g, x, k, op, ab, many=None):
+        if many is None:
+            x0 = x.clone()
+            fn = lambda: L.ogs_gather_scatter(g.handle, x.data_ptr(), k, tcode[x.dtype], op, 0, st.cuda_stream)
+            t = timeit(fn, restore=lambda: x.copy_(x0))
+        else:
+            arr = (C.c_void_p * len(many))(*[m.data_ptr() for m in many])
+            m0 = [m.clone() for m in many]
+            fn = lambda: L.ogs_gather_scatter_many(g.handle, arr, len(many), tcode[many[0].dtype], op, 0,
+                                                   st.cuda_stream)
+
+            def restore():
+                for m, q in zip(many, m0):
+                    m.copy_(q)
+            t = timeit(fn, restore=restore)
+        warm = timeit(fn, cold=False) if op == 0 else None
+        emit(case, g, k, t, ab, warm)
+
+    def idx_bytes(g):
+        return 4 * g.nnzT + 4 * (g.NlocalT + 1)
+
+    for p in range(1, 16):
+        ids = mesh.box_ids(24, 24, 24, p)
+        g = ogs.ogs_t().Setup(ids.size, ids.copy())
+        x = torch.from_numpy(mesh.uniform_values(ids.size, np.float64, -1, 1, p)).to(dev)
+        gs(f"24^3 p={p} f64 Add GS", g, x, 1, 0, 16 * ids.size + idx_bytes(g))
+        if p == 7:
+            gs("24^3 p=7 f32 Add GS", g, x.float(), 1, 0, 8 * ids.size + idx_bytes(g))
+            for dt in (torch.int32, torch.int64):
+                xi = torch.from_numpy(mesh.uniform_values(ids.size, np.int64, -(2 ** 30), 2 ** 30, 3)).to(dev).to(dt)
+                for op, nm in ((3, "Min"), (2, "Max")):
+                    gs(f"24^3 p=7 {str(dt)[6:]} {nm} GS", g, xi, 1, op, 2 * xi.element_size() * ids.size + idx_bytes(g))
+            sa = ids.copy()
+            sg = ogs.ogs_t().Setup(sa.size, sa, None, ogs.Signed, ogs.Auto, True)
+            gv = torch.zeros(sg.Ngather, dtype=torch.float64, device=dev)
+            abg = 8 * (ids.size + sg.Ngather) + idx_bytes(sg)
+            for nm, fn in (("Gather Trans", lambda: L.ogs_gather(sg.handle, gv.data_ptr(), x.data_ptr(), 1, 1, 0, 2,
+                                                                 st.cuda_stream)),
+                           ("Scatter NoTrans", lambda: L.ogs_scatter(sg.handle, x.data_ptr(), gv.data_ptr(), 1, 1, 1,
+                                                                     st.cuda_stream))):
+                emit(f"24^3 p=7 f64 {nm}", sg, 1, timeit(fn), abg, timeit(fn, cold=False))
+            del sg, gv
+        del g, x
+    ids = mesh.permute_elements(mesh.box_ids(32, 32, 16, 5), 5, seed=2024)
+    g = ogs.ogs_t().Setup(ids.size, ids.copy())
+    x1 = torch.from_numpy(mesh.uniform_values(ids.size, np.float64, -1, 1, 1)).to(dev)
+    gs("32x32x16 p=5 perm f64 Add k=1", g, x1, 1, 0, 16 * ids.size + idx_bytes(g))
+    for dt, s in ((torch.float64, 8), (torch.float32, 4)):
+        for op, nm, lo in ((0, "Add", -1.0), (1, "Mul", 0.5)):
+            hi = 1.0 if op == 0 else 2.0
+            x3 = torch.from_numpy(mesh.uniform_values(3 * ids.size, np.float64, lo, hi, 7)).to(dev).to(dt)
+            gs(f"32x32x16 p=5 perm {str(dt)[6:]} {nm} k=3", g, x3, 3, op, 6 * s * ids.size + idx_bytes(g))
+            vs = [torch.from_numpy(mesh.uniform_values(ids.size, np.float64, lo, hi, 70 + j)).to(dev).to(dt)
+                  for j in range(8)]
+            gs(f"32x32x16 p=5 perm {str(dt)[6:]} {nm} k=8 arrays", g, None, 8, op, 16 * s * ids.size + idx_bytes(g),
+               many=vs)
+    return 0
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         return run_reference(a)
+    if a.sweep:
+        return run_sweep(a)
     return run_ours(a)
 
 

@@ -93,9 +93,13 @@ constexpr size_t async_smem_bytes() {
   return static_cast<size_t>(kBlock / 32) * kAsyncStages * kWarpSlots * 32 * sizeof(T);
 }
 
-template <typename T, int OP, int MODE, int KL>
+// PLAIN: every member takes part and receives the result (Pattern all zero:
+// GatherScatter Sym, Gather/Scatter through the T map) -- the member-mask,
+// store-mode and gslib branches drop out at compile time.
+template <typename T, int OP, int MODE, int KL, bool PLAIN>
 __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const DevMaps m, const FieldArgs f,
-                                                                          const Pattern pat) {
+                                                                          const Pattern pat_in) {
+  const Pattern pat = PLAIN ? Pattern{0, 0, 0, 0} : pat_in;
   extern __shared__ __align__(16) unsigned char async_smem[];
   const int lane = static_cast<int>(threadIdx.x) & 31;
   const int warp = static_cast<int>(threadIdx.x) >> 5;
@@ -106,10 +110,10 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
   const int64_t nitems = nw * K;
   int64_t i = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + warp;
   if (i >= nitems) return;
-  const bool use_mask = (pat.gather_n || pat.scatter_n) && m.signed_maps;
-  const bool gmask = pat.gather_n != 0;
-  const int smode = pat.scatter_n;
-  const bool gslib = pat.gslib != 0;
+  const bool use_mask = !PLAIN && (pat.gather_n || pat.scatter_n) && m.signed_maps;
+  const bool gmask = !PLAIN && pat.gather_n != 0;
+  const int smode = PLAIN ? 0 : pat.scatter_n;
+  const bool gslib = !PLAIN && pat.gslib != 0;
   const int64_t stride = KL == kKInterleaved ? K : 1;
   auto tile_of = [&](int64_t item) {
     return static_cast<int>(KL == kKMany ? item % nw : (KL == kKInterleaved ? item / K : item));
@@ -199,7 +203,7 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
 #undef OGS_A_LOAD
 }
 
-template <typename T, int OP, int MODE, int KL>
+template <typename T, int OP, int MODE, int KL, bool PLAIN>
 inline int async_grid(int64_t nitems) {
   static int cached_dev = -1, cached = 0;
   int dev = 0;
@@ -208,9 +212,9 @@ inline int async_grid(int64_t nitems) {
     int bps = 0, sms = 0;
     // above 48 KB (more entries per lane) the dynamic shared memory must be opted into
     if (async_smem_bytes<T>() > 48 * 1024)
-      cudaFuncSetAttribute(ogs_async_kernel<T, OP, MODE, KL>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+      cudaFuncSetAttribute(ogs_async_kernel<T, OP, MODE, KL, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            static_cast<int>(async_smem_bytes<T>()));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_async_kernel<T, OP, MODE, KL>, kBlock,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_async_kernel<T, OP, MODE, KL, PLAIN>, kBlock,
                                                   async_smem_bytes<T>());
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cached = (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1);
@@ -222,8 +226,14 @@ inline int async_grid(int64_t nitems) {
 
 template <typename T, int OP, int MODE, int KL>
 inline void launch_async_kl(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
-  const int grid = async_grid<T, OP, MODE, KL>(static_cast<int64_t>(m.nwtiles) * (KL == kK1 ? 1 : f.K));
-  ogs_async_kernel<T, OP, MODE, KL><<<grid, kBlock, async_smem_bytes<T>(), s>>>(m, f, pat);
+  const int64_t nitems = static_cast<int64_t>(m.nwtiles) * (KL == kK1 ? 1 : f.K);
+  if (!pat.gather_n && !pat.scatter_n && !pat.limit_n && !pat.gslib) {
+    const int grid = async_grid<T, OP, MODE, KL, true>(nitems);
+    ogs_async_kernel<T, OP, MODE, KL, true><<<grid, kBlock, async_smem_bytes<T>(), s>>>(m, f, pat);
+  } else {
+    const int grid = async_grid<T, OP, MODE, KL, false>(nitems);
+    ogs_async_kernel<T, OP, MODE, KL, false><<<grid, kBlock, async_smem_bytes<T>(), s>>>(m, f, pat);
+  }
 }
 
 // Exact-degree tiles on the async pipeline, general tiles on the direct kernel.

@@ -52,30 +52,48 @@ struct Counters {
   int flags[3];
 };
 
+// Grid of the kernels that end in a global reduction: grid-stride loops, one
+// atomic per block, so a few hundred atomics meet on each counter instead of
+// one per warp.
+constexpr int kReduceBlocks = 1024;
+
+struct MaxOp {
+  template <typename T>
+  __device__ __forceinline__ T operator()(const T& a, const T& b) const {
+    return a > b ? a : b;
+  }
+};
+
+inline unsigned rblocks(int64_t n) {
+  const unsigned b = nblocks(n);
+  return b < kReduceBlocks ? b : kReduceBlocks;
+}
+
 // key = |id| (0 for zero ids), val = local index.
 __global__ void k_keys(const int64_t* __restrict__ ids, int64_t n, uint64_t* __restrict__ key,
                        int32_t* __restrict__ val, Counters* c) {
-  const int64_t i = static_cast<int64_t>(blockIdx.x) * kT + threadIdx.x;
-  uint64_t a = 0;
-  int zero = 0;
-  if (i < n) {
+  using RU = cub::BlockReduce<unsigned long long, kT>;
+  __shared__ typename RU::TempStorage tmp;
+  unsigned long long m = 0, zeros = 0;
+  int bad = 0;
+  for (int64_t i = static_cast<int64_t>(blockIdx.x) * kT + threadIdx.x; i < n;
+       i += static_cast<int64_t>(gridDim.x) * kT) {
     const int64_t id = ids[i];
-    if (id == INT64_MIN) atomicOr(&c->flags[0], 1);
-    a = static_cast<uint64_t>(id < 0 ? -id : id);
-    zero = (id == 0);
+    bad |= (id == INT64_MIN);
+    const uint64_t a = static_cast<uint64_t>(id < 0 ? -id : id);
+    zeros += (id == 0);
+    m = a > m ? a : m;
     key[i] = a;
     val[i] = static_cast<int32_t>(i);
   }
-  // one atomic per warp for each counter
-  unsigned long long m = a;
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long t = __shfl_down_sync(0xffffffffu, m, o);
-    m = t > m ? t : m;
-  }
-  const int zc = __popc(__ballot_sync(0xffffffffu, zero));
-  if ((threadIdx.x & 31) == 0) {
-    if (m) atomicMax(&c->maxkey, m);
-    if (zc) atomicAdd(&c->zeros, static_cast<unsigned long long>(zc));
+  const unsigned long long bm = RU(tmp).Reduce(m, MaxOp());
+  __syncthreads();
+  const unsigned long long bz = RU(tmp).Sum(zeros);
+  const int bbad = __syncthreads_or(bad);
+  if (threadIdx.x == 0) {
+    if (bm) atomicMax(&c->maxkey, bm);
+    if (bz) atomicAdd(&c->zeros, bz);
+    if (bbad) atomicOr(&c->flags[0], 1);
   }
 }
 
@@ -111,26 +129,25 @@ __global__ void k_group_heads(const int32_t* __restrict__ head, const int32_t* _
 __global__ void k_group_stats(const int32_t* __restrict__ gstart, const int32_t* __restrict__ pos_ex,
                               const int32_t* __restrict__ gfirst, int64_t ngroups, int32_t* __restrict__ gsize,
                               int32_t* __restrict__ gpos, uint64_t* __restrict__ mark, Counters* c) {
-  const int64_t g = static_cast<int64_t>(blockIdx.x) * kT + threadIdx.x;
-  int size = 0, undefined = 0;
-  if (g < ngroups) {
+  using RI = cub::BlockReduce<int, kT>;
+  __shared__ typename RI::TempStorage tmp;
+  int maxsize = 0, undefined = 0;
+  for (int64_t g = static_cast<int64_t>(blockIdx.x) * kT + threadIdx.x; g < ngroups;
+       g += static_cast<int64_t>(gridDim.x) * kT) {
     const int32_t s = gstart[g], e = gstart[g + 1];
-    size = e - s;
+    const int32_t size = e - s;
     const int32_t pc = pos_ex[e] - pos_ex[s];
     gsize[g] = size;
     gpos[g] = pc;
-    undefined = (pc != 1);
+    undefined |= (pc != 1);
+    maxsize = size > maxsize ? size : maxsize;
     mark[gfirst[g]] = pc > 0 ? uint64_t(1) : (uint64_t(1) << 32);
   }
-  int m = size;
-  for (int o = 16; o > 0; o >>= 1) {
-    const int t = __shfl_down_sync(0xffffffffu, m, o);
-    m = t > m ? t : m;
-  }
-  const unsigned u = __ballot_sync(0xffffffffu, undefined);
-  if ((threadIdx.x & 31) == 0) {
-    if (m) atomicMax(&c->flags[2], m);
-    if (u) atomicOr(&c->flags[1], 1);
+  const int bm = RI(tmp).Reduce(maxsize, MaxOp());
+  const int bu = __syncthreads_or(undefined);
+  if (threadIdx.x == 0) {
+    if (bm) atomicMax(&c->flags[2], bm);
+    if (bu) atomicOr(&c->flags[1], 1);
   }
 }
 
@@ -267,7 +284,7 @@ ogs_status build_device_maps(ogs_handle_s* h, int64_t N, int64_t* ids, int kind,
   e = cudaMemcpyAsync(d_ids, ids, static_cast<size_t>(N) * sizeof(int64_t), cudaMemcpyHostToDevice, st);
   if (!e) e = cudaMemsetAsync(d_c, 0, sizeof(Counters), st);
   if (e) return fail(e, "copy in");
-  k_keys<<<nblocks(N), kT, 0, st>>>(d_ids, N, key, val, d_c);
+  k_keys<<<rblocks(N), kT, 0, st>>>(d_ids, N, key, val, d_c);
   Counters c{};
   e = cudaMemcpyAsync(&c, d_c, sizeof(Counters), cudaMemcpyDeviceToHost, st);
   if (!e) e = cudaStreamSynchronize(st);
@@ -324,7 +341,7 @@ ogs_status build_device_maps(ogs_handle_s* h, int64_t N, int64_t* ids, int kind,
   if (!e) e = cudaMemsetAsync(mark, 0, static_cast<size_t>(N + 1) * sizeof(uint64_t), st);
   if (e) return fail(e, "memset");
   k_group_heads<<<nblocks(nnz), kT, 0, st>>>(head, gincl, sval, nnz, gstart, gfirst);
-  k_group_stats<<<nblocks(ngroups), kT, 0, st>>>(gstart, pos_ex, gfirst, ngroups, gsize, gpos, mark, d_c);
+  k_group_stats<<<rblocks(ngroups), kT, 0, st>>>(gstart, pos_ex, gfirst, ngroups, gsize, gpos, mark, d_c);
   if ((e = exclusive_sum(sc, mark, rank, N + 1, st))) return fail(e, "scan");
   uint64_t total = 0;
   e = cudaMemcpyAsync(&total, rank + N, sizeof(uint64_t), cudaMemcpyDeviceToHost, st);

@@ -17,9 +17,9 @@ namespace ogsgb {
 
 template <typename T, int OP, int MODE>
 inline cudaError_t launch_mode(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
-  if (OGS_KERNEL == 2) return launch_direct<T, OP, MODE>(m, f, pat, s);
-  if (OGS_ASYNC) return launch_async<T, OP, MODE>(m, f, pat, s);
-  return launch_warp<T, OP, MODE>(m, f, pat, s);
+  if constexpr (OGS_KERNEL == 2) return launch_direct<T, OP, MODE>(m, f, pat, s);
+  else if constexpr (OGS_ASYNC != 0) return launch_async<T, OP, MODE>(m, f, pat, s);
+  else return launch_warp<T, OP, MODE>(m, f, pat, s);
 }
 
 template <typename T, int MODE>
