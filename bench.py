@@ -37,7 +37,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "ogs_warp_kernel_gs_fp64_add_24x24x24_p7.md")
+PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "ogs_async_kernel_gs_fp64_add_24x24x24_p7.md")
 FALLBACK_HBM_GBS = 6800.0
 TYPE_CODE = {"float32": 0, "float64": 1, "int32": 2, "int64": 3}
 OP_CODE = {"add": 0, "mul": 1, "max": 2, "min": 3}
@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-meshes", type=int, default=256)
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-refdev", action="store_true")
     ap.add_argument("--served-requests", type=int, default=100000)
     ap.add_argument("--sweep", action="store_true",
                     help="print the results tables (one JSON line per case) instead of the bench line")
@@ -444,6 +445,38 @@ def run_ours(a):
     torch.cuda.synchronize(dev)
     warm_per_step = sum(e0.elapsed_time(e1) * 1e-3 for e0, e1 in wev) / a.steps
 
+    # the reference's device algorithm (OKL gatherScatter, 512-member row
+    # blocks) restated in CUDA, timed the same way on the same GPU
+    refdev_line = None
+    if not a.no_refdev and rank == 0:
+        import refdev
+        refdev.build()
+        rd = refdev.RefDevOgs(g)
+        rts = []
+        for it in range(a.warmup + a.steps):
+            work.copy_(pristine)
+            flush_l2()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rc = rd.gather_scatter(work.data_ptr(), a.k, tcode, ocode, stream.cuda_stream)
+            e1.record(stream)
+            if rc:
+                raise SystemExit(f"bench: refdev launch failed ({rc})")
+            torch.cuda.synchronize(dev)
+            if it >= a.warmup:
+                rts.append(e0.elapsed_time(e1) * 1e-3)
+        ref_out = work.clone()
+        work.copy_(pristine)
+        step()
+        torch.cuda.synchronize(dev)
+        same = bool(torch.equal(ref_out.view(torch.uint8), work.view(torch.uint8)))
+        rt = sum(rts) / len(rts)
+        refdev_line = {"what": "reference device algorithm (ogsKernels.okl gatherScatter, 512-member row blocks, "
+                               "256 threads, (blocks, k) grid) restated in CUDA, same GPU, same flush",
+                       "value": g.NgatherGlobal / rt, "unit": "DOFS/s", "ms_per_step": rt * 1e3,
+                       "row_blocks": rd.nblocks, "library_speedup": rt / per_step, "identical_results": same}
+        rd.free()
+
     # e2e through the C ABI host-buffer entry point, pinned host memory
     e2e = None
     if not a.no_e2e:
@@ -517,6 +550,7 @@ def run_ours(a):
         "batched": batched,
         "served": served,
         "setup": setup_s,
+        "reference_device_equivalent": refdev_line,
         "gpu_launches": a.steps,
         "clocks": clk.summary(),
         "wall_ms_per_step_incl_restore_and_flush": 1e3 * (w1 - w0) / a.steps,

@@ -123,14 +123,29 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
   };
   T* gv = static_cast<T*>(f.gv);
 
-  // prologue: state and gathers of item i, state of item i+W, descriptor of i+2W
+  // prologue: the descriptors of items i, i+W, i+2W in one round trip, the
+  // column ids of i and i+W in the next, then the gathers of item i; the
+  // loop's first pass issues the gathers of i+W at once
   int tcur = tile_of(i);
+  int tnxt = 0;
+  const bool has1 = i + W < nitems;
   Tile cur = m.wtiles[tcur];
+  Tile nxt{}, nn{};
+  if (has1) {
+    tnxt = tile_of(i + W);
+    nxt = m.wtiles[tnxt];
+    if (i + 2 * W < nitems) nn = m.wtiles[tile_of(i + 2 * W)];
+  }
   WarpState scur, snxt;
 #define OGS_A_LOAD(D, TILE, TI, S) warp_load_state<MODE, D>(m.b[D], TILE, m.wemask, TI, use_mask, pat, lane, S)
 #define OGS_A_LOAD_CUR(D) OGS_A_LOAD(D, cur, tcur, scur)
   OGS_DEGREE_SWITCH(cur.bucket, OGS_A_LOAD_CUR)
 #undef OGS_A_LOAD_CUR
+  if (has1) {
+#define OGS_A_LOAD_NXT(D) OGS_A_LOAD(D, nxt, tnxt, snxt)
+    OGS_DEGREE_SWITCH(nxt.bucket, OGS_A_LOAD_NXT)
+#undef OGS_A_LOAD_NXT
+  }
   {
     const int k0 = comp_of(i);
     const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, k0);
@@ -139,16 +154,6 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
 #undef OGS_A_ISSUE0
   }
   cp_async_commit();
-  Tile nxt{}, nn{};
-  int tnxt = 0;
-  if (i + W < nitems) {
-    tnxt = tile_of(i + W);
-    nxt = m.wtiles[tnxt];
-#define OGS_A_LOAD_NXT(D) OGS_A_LOAD(D, nxt, tnxt, snxt)
-    OGS_DEGREE_SWITCH(nxt.bucket, OGS_A_LOAD_NXT)
-#undef OGS_A_LOAD_NXT
-    if (i + 2 * W < nitems) nn = m.wtiles[tile_of(i + 2 * W)];
-  }
 
   int stage = 0;
   for (;;) {
