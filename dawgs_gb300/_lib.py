@@ -29,6 +29,8 @@ SIGNATURES = {
     "ogs_setup": (_i, [C.POINTER(_vp), _i64, _vp, _i, _i, _i, _i]),
     "ogs_setup_ex": (_i, [C.POINTER(_vp), _i64, _vp, _i, _i, _u]),
     "ogs_free": (_i, [_vp]),
+    "ogs_setup_maps": (_i, [C.POINTER(_vp), _i64, _i64, _i64, _vp, _vp, _vp, _vp, _u]),
+    "ogs_extract": (_i, [_i64, _i, _i, _vp, _vp, _vp, _vp]),
     "ogs_gather_scatter": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),
     "ogs_gather_scatter_many": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),
     "ogs_gather": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _vp]),

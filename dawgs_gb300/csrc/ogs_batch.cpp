@@ -119,6 +119,7 @@ ogs_status ogs_batch_create(ogs_batch* out, int type, const ogs_batch_entry* ent
     const char* bad = nullptr;
     if (!e.h) bad = "handle is NULL";
     else if (e.h->host_only) bad = "handle was set up host-only";
+    else if (!e.h->distinct_cols) bad = "a local node appears in two rows of this operator's map";
     else if (e.h->device != dev) bad = "handle lives on another device";
     else if (e.k < 1) bad = "k must be >= 1";
     else if (e.op < OGS_ADD || e.op > OGS_MIN) bad = "unknown op";

@@ -46,6 +46,14 @@ ogs_status check_common(ogs_handle h, int k, int type, int trans, const char* fn
   return OGS_OK;
 }
 
+// GatherScatter and Scatter write every member: refused when a local node
+// sits in two rows of an operator built from caller maps.
+ogs_status check_writes(ogs_handle h, const char* fn) {
+  if (!h->distinct_cols)
+    return set_error(OGS_EINVAL, std::string(fn) + ": a local node appears in two rows of this operator's map");
+  return OGS_OK;
+}
+
 ogs_status check_op(int op, const char* fn) {
   if (op < OGS_ADD || op > OGS_MIN) return set_error(OGS_EINVAL, std::string(fn) + ": unknown op");
   return OGS_OK;
@@ -281,6 +289,7 @@ ogs_status ogs_free(ogs_handle h) {
 ogs_status ogs_gather_scatter(ogs_handle h, void* d_v, int k, int type, int op, int trans, void* stream) {
   const char* fn = "ogs_gather_scatter";
   ogs_status s = check_common(h, k, type, trans, fn);
+  if (s == OGS_OK) s = check_writes(h, fn);
   if (s == OGS_OK) s = check_op(op, fn);
   if (s != OGS_OK) return s;
   if (h->N == 0) return OGS_OK;
@@ -295,6 +304,7 @@ ogs_status ogs_gather_scatter_many(ogs_handle h, void* const* d_vs, int k, int t
                                    void* stream) {
   const char* fn = "ogs_gather_scatter_many";
   ogs_status s = check_common(h, k, type, trans, fn);
+  if (s == OGS_OK) s = check_writes(h, fn);
   if (s == OGS_OK) s = check_op(op, fn);
   if (s != OGS_OK) return s;
   if (h->N == 0) return OGS_OK;
@@ -334,6 +344,7 @@ ogs_status ogs_gather(ogs_handle h, void* d_gv, const void* d_v, int k, int type
 ogs_status ogs_scatter(ogs_handle h, void* d_v, const void* d_gv, int k, int type, int trans, void* stream) {
   const char* fn = "ogs_scatter";
   ogs_status s = check_common(h, k, type, trans, fn);
+  if (s == OGS_OK) s = check_writes(h, fn);
   if (s != OGS_OK) return s;
   if (!h->gather_defined)  // AssertGatherDefined in ScatterStart, ogs.cpp:398
     return set_error(OGS_EUNDEFINED, "Gather operation not well-defined.");
@@ -349,6 +360,7 @@ ogs_status ogs_scatter(ogs_handle h, void* d_v, const void* d_gv, int k, int typ
 ogs_status ogs_gather_scatter_host(ogs_handle h, void* v, int k, int type, int op, int trans, void* stream) {
   const char* fn = "ogs_gather_scatter_host";
   ogs_status s = check_common(h, k, type, trans, fn);
+  if (s == OGS_OK) s = check_writes(h, fn);
   if (s == OGS_OK) s = check_op(op, fn);
   if (s != OGS_OK) return s;
   if (h->N == 0) return OGS_OK;
@@ -448,6 +460,7 @@ ogs_status ogs_gather_host(ogs_handle h, void* gv, const void* v, int k, int typ
 ogs_status ogs_scatter_host(ogs_handle h, void* v, const void* gv, int k, int type, int trans, void* stream) {
   const char* fn = "ogs_scatter_host";
   ogs_status s = check_common(h, k, type, trans, fn);
+  if (s == OGS_OK) s = check_writes(h, fn);
   if (s != OGS_OK) return s;
   if (!h->gather_defined) return set_error(OGS_EUNDEFINED, "Gather operation not well-defined.");
   if (h->N == 0 || h->NlocalT == 0) return OGS_OK;

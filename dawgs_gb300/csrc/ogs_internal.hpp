@@ -199,6 +199,8 @@ struct ogs_handle_s {
   bool host_only = false;
   bool covers_all = false;  // every local node is in the T map (no zero ids)
   bool gslib = false;       // maps in gslib's member order (ogs_gslib.cpp)
+  bool from_maps = false;   // an operator over caller-built maps (ogs_maps.cpp)
+  bool distinct_cols = true;  // no local node in two rows (GatherScatter/Scatter need it)
 
   std::vector<int32_t> rowStartsT, colIdsT, rowStartsN, colIdsN;  // N empty when Unsigned
   ogsgb::HostLayout lay;

@@ -72,6 +72,8 @@ extern "C" ogs_status ogs_gather_scatter_host_noalloc(ogs_handle h, void* v, int
   const char* fn = "ogs_gather_scatter_host_noalloc";
   if (!h) return set_error(OGS_EINVAL, std::string(fn) + ": handle is NULL");
   if (h->host_only) return set_error(OGS_EINVAL, std::string(fn) + ": handle was set up host-only");
+  if (!h->distinct_cols)
+    return set_error(OGS_EINVAL, std::string(fn) + ": a local node appears in two rows of this operator's map");
   if (k < 1) return set_error(OGS_EINVAL, std::string(fn) + ": k must be >= 1");
   if (type < OGS_FLOAT || type > OGS_INT64) return set_error(OGS_EINVAL, std::string(fn) + ": unknown type");
   if (op < OGS_ADD || op > OGS_MIN) return set_error(OGS_EINVAL, std::string(fn) + ": unknown op");

@@ -353,6 +353,8 @@ ogs_status ogs_server_add_mesh(ogs_server s, ogs_handle h, int* mesh_id) {
   if (!s || !h || !mesh_id) return set_error(OGS_EINVAL, "ogs_server_add_mesh: NULL argument");
   if (h->host_only || h->device != s->device)
     return set_error(OGS_EINVAL, "ogs_server_add_mesh: the handle must live on the server's device");
+  if (!h->distinct_cols)
+    return set_error(OGS_EINVAL, "ogs_server_add_mesh: a local node appears in two rows of this operator's map");
   std::lock_guard<std::mutex> g(s->mu);
   s->meshes.push_back(h);
   *mesh_id = static_cast<int>(s->meshes.size()) - 1;

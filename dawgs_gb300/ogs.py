@@ -104,6 +104,16 @@ def _stream_of(stream):
     return None
 
 
+def extract(out, q, ids, k, stream=None):
+    """out[n*k+c] = q[ids[n]*k+c]: the exchange's send-buffer packing
+    (ogsKernels.okl:167-177).  Device tensors; ids int32."""
+    t = _type_of(q)
+    if _type_of(out) != t:
+        raise OgsError(_lib.OGS_EINVAL, "out and q must have the same dtype")
+    check(lib().ogs_extract(int(ids.numel()), int(k), int(t), _ptr(ids), _ptr(q), _ptr(out), _stream_of(stream)))
+    return out
+
+
 class ogs_t:
     """One single-rank gather-scatter handle (ogs::ogs_t)."""
 
@@ -134,8 +144,33 @@ class ogs_t:
         flags |= {None: 0, "device": _lib.SETUP_DEVICE_MAPS, "host": _lib.SETUP_HOST_MAPS}[maps]
         check(lib().ogs_setup_ex(C.byref(h), int(N), ids.ctypes.data, int(kind), int(bool(unique)), flags))
         self._h = h
+        return self._refresh()
+
+    def SetupMaps(self, N, rowStartsT, colIdsT, rowStartsN=None, colIdsN=None, NrowsN=None, host_only=False):
+        """An operator over caller-built CSR maps (ogsOperator_t: the
+        reference's gatherLocal, gatherHalo and postmpi are such operators).
+        Without N maps the N map is the T map."""
+        self.Free()
+        i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+        rsT, ciT = i32(rowStartsT), i32(colIdsT)
+        NrowsT = rsT.size - 1
+        rsN = ciN = None
+        if rowStartsN is not None:
+            rsN, ciN = i32(rowStartsN), i32(colIdsN if colIdsN is not None else [])
+            if NrowsN is None:
+                NrowsN = NrowsT
+        h = C.c_void_p()
+        flags = _lib.SETUP_HOST_ONLY if host_only else 0
+        check(lib().ogs_setup_maps(C.byref(h), int(N), int(NrowsN if NrowsN is not None else NrowsT), int(NrowsT),
+                                   rsN.ctypes.data if rsN is not None else None,
+                                   ciN.ctypes.data if ciN is not None and ciN.size else None,
+                                   rsT.ctypes.data, ciT.ctypes.data if ciT.size else None, flags))
+        self._h = h
+        return self._refresh()
+
+    def _refresh(self):
         c = OgsCounts()
-        check(lib().ogs_get_counts(h, C.byref(c)))
+        check(lib().ogs_get_counts(self._h, C.byref(c)))
         self.N, self.Ngather, self.NgatherGlobal = c.N, c.Ngather, c.NgatherGlobal
         self.NlocalP, self.NlocalT = c.NlocalP, c.NlocalT
         self.nnzT, self.nnzN = c.nnzT, c.nnzN

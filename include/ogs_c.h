@@ -155,6 +155,31 @@ ogs_status ogs_get_maps(ogs_handle h, int32_t *rowStartsT, int32_t *colIdsT,
 /* Degree buckets and tiles the kernels run over (no reference counterpart). */
 ogs_status ogs_get_layout_stats(ogs_handle h, ogs_layout_stats *out);
 
+/* ---- pieces of the multi-rank path that run on the device ----
+ * An operator over caller-built CSR maps: the reference's ogsOperator_t
+ * (include/ogs/ogsOperator.hpp:40-120), of which its multi-rank setup makes
+ * gatherLocal, gatherHalo (libs/ogs/ogsSetup.cpp:569-776) and the exchange's
+ * postmpi (libs/ogs/ogsAllToAll.cpp:255-331).  The T map (rowStartsT[NrowsT+1],
+ * colIdsT) is required; colIds lie in [0, N).  rowStartsN == NULL makes the N
+ * map the T map (Unsigned); otherwise rowStartsN has NrowsT+1 entries, rows at
+ * and above NrowsN are empty and each row's N members are a subsequence of its
+ * T members.  The handle takes ogs_gather / ogs_scatter / ogs_gather_scatter
+ * (and the _host, _many forms) like one from ogs_setup, with no
+ * gather-defined check (an operator has none); GatherScatter and Scatter are
+ * refused when a local node sits in two rows.  ogs_gather may run in place
+ * (d_gv == d_v) when no row reads an entry another row's result overwrites:
+ * postmpi's maps (row n = own entry n, then received entries) are such.
+ * flags: OGS_SETUP_HOST_ONLY or 0. */
+ogs_status ogs_setup_maps(ogs_handle *out, int64_t N, int64_t NrowsN, int64_t NrowsT,
+                          const int32_t *rowStartsN, const int32_t *colIdsN,
+                          const int32_t *rowStartsT, const int32_t *colIdsT, unsigned flags);
+/* Send-buffer packing, out[n*k+c] = q[ids[n]*k+c] for n < N: the reference's
+ * extract kernel (libs/ogs/okl/ogsKernels.okl:167-177) as the all-to-all
+ * exchange runs it before sending (libs/ogs/ogsAllToAll.cpp:126-131).
+ * Device pointers; asynchronous on `stream`. */
+ogs_status ogs_extract(int64_t N, int k, int type, const int32_t *d_ids, const void *d_q, void *d_out,
+                       void *stream);
+
 /* ---- gslib-compatible entry points ----
  * gslib (3rdParty/gslib of the reference) is the gather-scatter that dawgs
  * checks ogs against (dawgsGS.cpp:34-105).  These calls give its single-rank

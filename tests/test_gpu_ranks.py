@@ -1,0 +1,100 @@
+"""Emulated multi-rank GatherScatter on the GPU (dawgs_gb300/ranks.py): every
+rank's gatherLocal, gatherHalo and postmpi are library operators built from
+maps (ogs_setup_maps), the send buffers are packed and the exchange is done
+by ogs_extract, and postmpi's Gather runs in place.  The fields equal the
+oracle's restatement of the reference's multi-rank fold order bit for bit, and
+the single-rank result of the whole mesh exactly for integer types and
+Max/Min (within rounding for floating-point Add and Mul, whose order the rank
+split changes)."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from dawgs_gb300 import mesh, ogs, ranks
+from helpers import first_diff, same_bits, values
+from oracle import ranks as oranks
+
+pytestmark = pytest.mark.gpu
+
+PARTS = [((6, 5, 4, 3), 2, "slabs"), ((6, 5, 4, 3), 3, "random"), ((5, 4, 4, 2), 4, "random"),
+         ((8, 4, 4, 2), 8, "slabs"), ((4, 4, 3, 1), 5, "random")]
+
+
+@pytest.fixture(scope="module")
+def setups(cuda):
+    out = {}
+    for box, R, how in PARTS:
+        parts = oranks.partition_box(*box, R, how=how, seed=17)
+        out[(box, R, how)] = (parts, ranks.ranks_ogs_t(parts))
+    return out
+
+
+@pytest.mark.parametrize("key", PARTS, ids=lambda p: f"{p[0]}-{p[1]}-{p[2]}")
+@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int32, np.int64], ids=lambda t: np.dtype(t).name)
+@pytest.mark.parametrize("op", ["add", "mul", "max", "min"])
+def test_ranks_match_oracle(setups, oracle_mod, key, dtype, op):
+    parts, rk = setups[key]
+    for k in (1, 3):
+        vs = [values(k * p.size, dtype, op, seed=40 + i + 7 * k) for i, p in enumerate(parts)]
+        want = oranks.ranks_gather_scatter(parts, vs, k, op)
+        ds = [torch.from_numpy(v.copy()).cuda() for v in vs]
+        rk.GatherScatter(ds, k, ogs.Op[op.capitalize()])
+        torch.cuda.synchronize()
+        for r, (d, w) in enumerate(zip(ds, want)):
+            got = d.cpu().numpy()
+            assert same_bits(got, w), (key, k, r, first_diff(got, w))
+        if np.dtype(dtype).kind == "i" or op in ("max", "min"):
+            # the rank split does not change exact folds: whole-mesh single-rank result
+            g = np.concatenate(parts)
+            single = oracle.OracleOgs(g.copy(), "unsigned").gather_scatter(np.concatenate(vs), k, op, "sym")
+            assert same_bits(np.concatenate([d.cpu().numpy() for d in ds]), single)
+
+
+def test_ranks_float_add_close_to_single_rank(setups, oracle_mod):
+    parts, rk = setups[((5, 4, 4, 2), 4, "random")]
+    vs = [values(p.size, np.float64, "add", seed=3 + i) for i, p in enumerate(parts)]
+    ds = [torch.from_numpy(v.copy()).cuda() for v in vs]
+    rk.GatherScatter(ds, 1, ogs.Add)
+    single = oracle.OracleOgs(np.concatenate(parts), "unsigned").gather_scatter(np.concatenate(vs), 1, "add", "sym")
+    got = np.concatenate([d.cpu().numpy() for d in ds])
+    assert np.allclose(got, single, rtol=1e-13, atol=1e-15)  # fp64 Add, fold order changed by the split
+
+
+def test_ranks_larger_mesh_start_finish(oracle_mod, cuda):
+    """12^3 p=4 over 8 ranks (random elements), Start and Finish called apart."""
+    parts = oranks.partition_box(12, 12, 12, 4, 8, how="random", seed=5)
+    rk = ranks.ranks_ogs_t(parts)
+    vs = [values(p.size, np.float64, "add", seed=60 + i) for i, p in enumerate(parts)]
+    want = oranks.ranks_gather_scatter(parts, vs, 1, "add")
+    ds = [torch.from_numpy(v.copy()).cuda() for v in vs]
+    rk.GatherScatterStart(ds, 1, ogs.Add)
+    rk.GatherScatterFinish(ds, 1, ogs.Add)
+    torch.cuda.synchronize()
+    for d, w in zip(ds, want):
+        assert same_bits(d.cpu().numpy(), w)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int32, np.int64], ids=lambda t: np.dtype(t).name)
+def test_extract(cuda, dtype):
+    rng = np.random.default_rng(1)
+    for k in (1, 3):
+        q = values(1000 * k, dtype, "add", seed=2)
+        ids = rng.integers(0, 1000, 777).astype(np.int32)
+        out = torch.zeros(777 * k, dtype=torch.from_numpy(q).dtype, device="cuda")
+        ogs.extract(out, torch.from_numpy(q).cuda(), torch.from_numpy(ids).cuda(), k)
+        want = q.reshape(1000, k)[ids].reshape(-1)
+        assert same_bits(out.cpu().numpy(), want)
+
+
+def test_operator_with_shared_column_refuses_writes(cuda):
+    g = ogs.ogs_t().SetupMaps(4, [0, 2, 4], [0, 1, 1, 3])   # local node 1 in two rows
+    v = torch.ones(4, dtype=torch.float64, device="cuda")
+    gv = torch.zeros(2, dtype=torch.float64, device="cuda")
+    g.Gather(gv, v, 1, ogs.Add, ogs.Trans)
+    torch.cuda.synchronize()
+    assert gv.cpu().tolist() == [2.0, 2.0]
+    with pytest.raises(ogs.OgsError):
+        g.GatherScatter(v, 1, ogs.Add, ogs.Sym)
+    with pytest.raises(ogs.OgsError):
+        g.Scatter(v, gv, 1, ogs.Trans)
