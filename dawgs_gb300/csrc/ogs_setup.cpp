@@ -192,7 +192,9 @@ void build_layout(ogs_handle_s* h) {
   int64_t gnnzT = 0, gnnzN = 0;
   for (int64_t r = 0; r < R; ++r) {
     const int d = rsT[r + 1] - rsT[r];
-    if (d <= kDmax) cnt[d]++;
+    // rows without members (possible in operators built from caller maps) go
+    // to the general bucket: a Gather still writes the op identity there
+    if (d >= 1 && d <= kDmax) cnt[d]++;
     else { cnt[0]++; gnnzT += d; gnnzN += rsN[r + 1] - rsN[r]; }
   }
   int64_t stride[kDmax + 1] = {0};
@@ -213,7 +215,7 @@ void build_layout(ogs_handle_s* h) {
   for (int64_t r = 0; r < R; ++r) {
     const int32_t s = rsT[r], d = rsT[r + 1] - s;
     const bool inP = r < h->NlocalP;
-    if (d <= kDmax) {
+    if (d >= 1 && d <= kDmax) {
       const int64_t i = fill[d]++;
       const int64_t n = stride[d];
       L.rows[d][i] = static_cast<int32_t>(r);

@@ -2,34 +2,49 @@
 process on one GPU: the device half of the path a multi-rank caller runs.
 
 At several ranks the reference splits each rank's rows into local rows (ids on
-this rank only) and halo rows (ids shared with other ranks), and a
+this rank only) and halo rows (ids shared with other ranks), and an ogs_t
 GatherScatter becomes (libs/ogs/ogs.cpp:39-123, ogsAllToAll.cpp:126-175):
 
-  Start:  halo Gather   haloBuf[h] = fold of the rank's members of halo row h
-          extract       sendBuf[n] = haloBuf[sendIds[n]]       (ogsKernels.okl:167-177)
-          exchange      all-to-all of the send buffers into each rank's
-                        receive region haloBuf[Nhalo:]           (MPI in the reference)
+  Start:  halo Gather    haloBuf[h] = fold of the rank's members of halo row h
+          extract        sendBuf[n] = haloBuf[sendIds[n]]      (ogsKernels.okl:167-177)
+          exchange       all-to-all of the send buffers into each rank's
+                         receive region haloBuf[Nhalo:]          (MPI in the reference)
   Finish: local GatherScatter over the local rows (overlapping the exchange)
           postmpi Gather haloBuf[h] = fold(haloBuf[h], received partials of h)
-          halo Scatter  every member of halo row h gets haloBuf[h]
+          halo Scatter   the members of halo row h get haloBuf[h]
+
+A halo_t (kind Halo, libs/ogs/ogsHalo.cpp:39-359) runs the same halo steps
+without local rows: Exchange with Add/NoTrans (the owner's value goes to
+every copy), Combine with Add/Trans (every copy's value is summed into the
+owner's).  NoTrans gathers the N members (positive ids) and sends only from
+ranks that hold one; Trans and Sym gather all members; the Scatter writes the
+T members (NoTrans, Sym) or the N members (Trans) (ogsOperator.cpp:60-360).
 
 Here every rank's operators are library handles built from maps
-(ogs_setup_maps), the packing is ogs_extract, and the exchange -- a network
-step in the reference -- is one more ogs_extract per rank that gathers its
+(ogs_setup_maps), the packing is ogs_extract, and the exchange -- the network
+step of the reference -- is one more ogs_extract per rank, gathering its
 receive region from the concatenated send buffers of all ranks.  The maps
-follow the reference's construction for Unsigned handles
-(ogsSetup.cpp:333-566 ConstructSharedNodes, 686-776 LocalUnsignedSetup;
-ogsAllToAll.cpp:178-331): rows numbered by first appearance on the rank, local
-and halo rows separately; members in ascending local index; each rank sends
-its halo rows to every other rank holding the same id, ordered by
-(destination rank, row); a rank receives from the source ranks in ascending
-order; postmpi row h lists h itself, then its received entries in receive
-order.  So a halo row folds the rank's own partial first, then the other
-ranks' partials by ascending rank -- the reference's order.
+follow the reference's construction (ogsSetup.cpp:333-566
+ConstructSharedNodes, 569-846 Local*Setup; ogsAllToAll.cpp:178-331):
 
-The reference distributes ids to ranks by |id| % size and sorts across ranks
-to find shared ids; with all ranks in one process the shared ids come from one
-pass over all ranks' ids instead.  Only Unsigned handles are emulated.
+* rows by first appearance on the rank, in four classes numbered apart:
+  local rows with a positive member, then the other local rows; halo rows with
+  a positive member on this rank, then the other halo rows;
+* members in ascending local index; N members: ids > 0 (Signed), all members
+  of a halo row whose group's positive id is on this rank (Halo), all
+  (Unsigned);
+* a rank sends each halo row to every other holder of its id, ordered by
+  (destination, row); the N sends are the rows with a positive member;
+* a rank receives from the source ranks in ascending order;
+* postmpi T row h = [h, its received T entries]; postmpi N row h = [h if the
+  row has a positive member, its received N entries], over a compact N receive
+  region.  The library wants an N map inside the T map, so the two postmpi maps
+  are two operators here.
+
+A halo row therefore folds the rank's own partial first, then the other
+ranks' partials by ascending rank -- the reference's order.  The reference
+distributes ids by |id| % size and sorts across ranks to find the shared ones;
+with all ranks in one process one pass over all ranks' ids finds them.
 """
 from __future__ import annotations
 
@@ -37,11 +52,16 @@ import numpy as np
 
 from . import ogs
 
+UNSIGNED, SIGNED, HALO = int(ogs.Unsigned), int(ogs.Signed), int(ogs.Halo)
 
-def _csr(rows_of_members, nrows):
-    """T map with members of each row in ascending local index:
-    rows_of_members[n] = row of local node n, or -1."""
-    n = np.nonzero(rows_of_members >= 0)[0]
+
+def _csr(rows_of_members, nrows, keep=None):
+    """CSR map with members of each row in ascending local index:
+    rows_of_members[n] = row of local node n, or -1; keep: optional mask."""
+    sel = rows_of_members >= 0
+    if keep is not None:
+        sel &= keep
+    n = np.nonzero(sel)[0]
     r = rows_of_members[n]
     order = np.argsort(r, kind="stable")  # stable: members stay in ascending local index
     counts = np.bincount(r, minlength=nrows)
@@ -50,156 +70,251 @@ def _csr(rows_of_members, nrows):
     return starts.astype(np.int32), n[order].astype(np.int32)
 
 
-def build_rank_maps(ids_list):
-    """Per-rank maps of the emulated multi-rank Unsigned setup.
+def _number_rows(first, positive, members):
+    """The groups `members` (indices into uniq) split into positive and other
+    groups, each in order of first appearance: rows are numbered positive
+    groups first (ogsSetup.cpp:406-433)."""
+    pos = members[positive[members]]
+    neg = members[~positive[members]]
+    pos = pos[np.argsort(first[pos], kind="stable")]
+    neg = neg[np.argsort(first[neg], kind="stable")]
+    return pos, neg
 
-    Returns a list of dicts (one per rank) with: N, local (rowStarts, colIds),
-    halo (rowStarts, colIds), halo_ids (|id| of each halo row), send_ids
-    (halo rows in send order), send_counts[R], recv_counts[R], recv_rows
-    (the local halo row of each received entry, receive order), post
-    (rowStarts, colIds) over [halo rows | received entries]."""
+
+def build_rank_maps(ids_list, kind=UNSIGNED):
+    """Per-rank maps of the emulated multi-rank setup (see the module text).
+
+    Each rank's dict: N, nlocal, nlocalP, local (rsT, ciT, rsN, ciN), nhalo,
+    nhaloP, halo (rsT, ciT, rsN, ciN), halo_ids, send_T, send_N (halo rows in
+    send order), send_counts_T/N[R], recv_rows_T/N, postT (rs, ci) over
+    nhalo + len(recv_rows_T) columns, postN (rs, ci) over nhalo +
+    len(recv_rows_N) columns."""
+    if kind not in (UNSIGNED, SIGNED, HALO):
+        raise ValueError("kind must be Unsigned, Signed or Halo")
     R = len(ids_list)
-    absids = [np.abs(np.asarray(x, dtype=np.int64)) for x in ids_list]
-    # ranks holding each id
+    ids_list = [np.asarray(x, dtype=np.int64) for x in ids_list]
+    absids = [np.abs(x) for x in ids_list]
     per_rank = [np.unique(a[a != 0]) for a in absids]
     allids = np.concatenate(per_rank) if per_rank else np.zeros(0, np.int64)
     ids_u, nranks = np.unique(allids, return_counts=True)
     shared_ids = ids_u[nranks > 1]
+    if kind == HALO:
+        # every id group needs exactly one positive id over all ranks (ogsSetup.cpp:293-296)
+        pos_all = np.concatenate([x[x > 0] for x in ids_list]) if R else np.zeros(0, np.int64)
+        u, c = np.unique(pos_all, return_counts=True)
+        cnt = np.zeros(ids_u.size, np.int64)
+        cnt[np.searchsorted(ids_u, u)] = c
+        bad = ids_u[cnt != 1]
+        if bad.size:
+            raise ValueError(f"Halo setup: id {int(bad[0])} has {int(cnt[cnt != 1][0])} positive copies, not 1")
     out = []
-    for r, a in enumerate(absids):
+    for r in range(R):
+        a, x = absids[r], ids_list[r]
         nz = np.nonzero(a)[0]
         uniq, first = np.unique(a[nz], return_index=True)
         first = nz[first]
+        node_uniq = np.full(a.size, -1, np.int64)
+        node_uniq[nz] = np.searchsorted(uniq, a[nz])
         is_sh = np.isin(uniq, shared_ids)
-        # rows by first appearance, local and halo rows separately (ogsSetup.cpp:406-433)
-        loc = np.nonzero(~is_sh)[0]
-        hal = np.nonzero(is_sh)[0]
-        loc = loc[np.argsort(first[loc], kind="stable")]
-        hal = hal[np.argsort(first[hal], kind="stable")]
-        row_of_uniq = np.empty(uniq.size, np.int64)
-        row_of_uniq[loc] = np.arange(loc.size)
-        row_of_uniq[hal] = np.arange(hal.size)
-        node_uniq = np.searchsorted(uniq, a[nz])
+        has_pos = np.zeros(uniq.size, bool)
+        if kind == UNSIGNED:
+            has_pos[:] = True
+        else:
+            has_pos[np.unique(node_uniq[nz][x[nz] > 0])] = True
+        loc_p, loc_n = _number_rows(first, has_pos, np.nonzero(~is_sh)[0])
+        hal_p, hal_n = _number_rows(first, has_pos, np.nonzero(is_sh)[0])
+        if kind == HALO:
+            loc_p = loc_p[:0]
+            loc_n = loc_n[:0]
+        row_of = np.full(uniq.size, -1, np.int64)
+        row_of[np.concatenate([loc_p, loc_n])] = np.arange(loc_p.size + loc_n.size)
+        row_of[np.concatenate([hal_p, hal_n])] = np.arange(hal_p.size + hal_n.size)
         rows_local = np.full(a.size, -1, np.int64)
         rows_halo = np.full(a.size, -1, np.int64)
-        m_loc = ~is_sh[node_uniq]
-        rows_local[nz[m_loc]] = row_of_uniq[node_uniq[m_loc]]
-        rows_halo[nz[~m_loc]] = row_of_uniq[node_uniq[~m_loc]]
-        out.append({"N": int(a.size), "local": _csr(rows_local, loc.size), "halo": _csr(rows_halo, hal.size),
-                    "halo_ids": uniq[hal], "nhalo": int(hal.size)})
-    # exchange: rank r sends halo row h (id b) to every other rank j holding b,
-    # ordered by (j, h) (ogsAllToAll.cpp:185-245)
+        member_sh = np.zeros(a.size, bool)
+        member_sh[nz] = is_sh[node_uniq[nz]]
+        if kind != HALO:
+            m = ~member_sh
+            m[a == 0] = False
+            rows_local[m] = row_of[node_uniq[m]]
+        rows_halo[member_sh] = row_of[node_uniq[member_sh]]
+        # N members
+        if kind == UNSIGNED:
+            nmem = a != 0
+        elif kind == SIGNED:
+            nmem = x > 0
+        else:  # Halo: every member of a row whose positive id is on this rank
+            nmem = np.zeros(a.size, bool)
+            nmem[nz] = has_pos[node_uniq[nz]]
+        nl, nh = loc_p.size + loc_n.size, hal_p.size + hal_n.size
+        local = _csr(rows_local, nl) + _csr(rows_local, nl, nmem)
+        halo = _csr(rows_halo, nh) + _csr(rows_halo, nh, nmem)
+        order_h = np.concatenate([hal_p, hal_n])
+        out.append({"N": int(a.size), "nlocal": int(nl), "nlocalP": int(loc_p.size), "local": local,
+                    "nhalo": int(nh), "nhaloP": int(hal_p.size), "halo": halo,
+                    "halo_ids": uniq[order_h], "halo_pos": has_pos[order_h]})
+    # exchange: rank r sends halo row h (id b) to every other holder j,
+    # ordered by (j, h); N sends are the rows with a positive member
     holders = {}
     for r, m in enumerate(out):
         for h, b in enumerate(m["halo_ids"]):
-            holders.setdefault(int(b), []).append((r, h))
-    sends = [[[] for _ in range(R)] for _ in range(R)]  # sends[r][j] = [(h_r, h_j)]
-    for b, lst in holders.items():
-        for r, hr in lst:
-            for j, hj in lst:
+            holders.setdefault(int(b), []).append((r, h, bool(m["halo_pos"][h])))
+    sends = [[[] for _ in range(R)] for _ in range(R)]  # sends[r][j] = [(h_r, h_j, positive on r)]
+    for lst in holders.values():
+        for r, hr, pr in lst:
+            for j, hj, _ in lst:
                 if j != r:
-                    sends[r][j].append((hr, hj))
+                    sends[r][j].append((hr, hj, pr))
     for r in range(R):
-        send_ids, counts = [], []
+        sT, sN, cT, cN = [], [], [], []
         for j in range(R):
             sends[r][j].sort()
-            send_ids += [hr for hr, _ in sends[r][j]]
-            counts.append(len(sends[r][j]))
-        out[r]["send_ids"] = np.asarray(send_ids, np.int32)
-        out[r]["send_counts"] = np.asarray(counts, np.int64)
-    # receive order: source ranks ascending, each source in its send order
+            sT += [hr for hr, _, _ in sends[r][j]]
+            sN += [hr for hr, _, p in sends[r][j] if p]
+            cT.append(len(sends[r][j]))
+            cN.append(sum(1 for _, _, p in sends[r][j] if p))
+        m = out[r]
+        m["send_T"], m["send_N"] = np.asarray(sT, np.int32), np.asarray(sN, np.int32)
+        m["send_counts_T"], m["send_counts_N"] = np.asarray(cT, np.int64), np.asarray(cN, np.int64)
     for j in range(R):
-        recv_rows, recv_src = [], []
-        for r in range(R):
-            recv_rows += [hj for _, hj in sends[r][j]]
         m = out[j]
-        m["recv_rows"] = np.asarray(recv_rows, np.int64)
-        m["recv_counts"] = np.asarray([len(sends[r][j]) for r in range(R)], np.int64)
-        nh = m["nhalo"]
-        # postmpi: row h = [h, Nhalo + p for received p of row h, in receive order]
-        rows = np.concatenate([np.arange(nh), m["recv_rows"]])
-        m["post"] = _csr(rows, nh)
-        m["post_cols"] = nh + len(recv_rows)
+        rT = [hj for r in range(R) for _, hj, _ in sends[r][j]]
+        rN = [hj for r in range(R) for _, hj, p in sends[r][j] if p]
+        m["recv_rows_T"], m["recv_rows_N"] = np.asarray(rT, np.int64), np.asarray(rN, np.int64)
+        nh, nhp = m["nhalo"], m["nhaloP"]
+        m["postT"] = _csr(np.concatenate([np.arange(nh), m["recv_rows_T"]]), nh)
+        m["postN"] = _csr(np.concatenate([np.arange(nhp), np.full(nh - nhp, -1), m["recv_rows_N"]]), nh)
+        m["postT_cols"] = nh + len(rT)
+        m["postN_cols"] = nh + len(rN)
     return out
 
 
 class ranks_ogs_t:
-    """GatherScatter over R emulated ranks on one device.
+    """ogs_t GatherScatter (kind Unsigned or Signed) and halo_t
+    Exchange/Combine (kind Halo) over R emulated ranks on one device.
 
     ids_list: one int64 id array per rank.  Fields: one device tensor per rank
     (k interleaved components), all of one dtype."""
 
-    def __init__(self, ids_list):
+    def __init__(self, ids_list, kind=UNSIGNED):
         import torch
         self.R = len(ids_list)
-        self.maps = build_rank_maps(ids_list)
-        self.local, self.halo, self.post = [], [], []
+        self.kind = int(kind)
+        self.maps = build_rank_maps(ids_list, self.kind)
+        self.local, self.halo, self.postT, self.postN = [], [], [], []
         for m in self.maps:
-            self.local.append(ogs.ogs_t().SetupMaps(m["N"], *m["local"]))
-            self.halo.append(ogs.ogs_t().SetupMaps(m["N"], *m["halo"]))
-            self.post.append(ogs.ogs_t().SetupMaps(m["post_cols"], *m["post"]))
-        # send buffers of all ranks, concatenated; each rank's receive region
-        # gathers from it (the exchange)
-        self.send_off = np.zeros(self.R + 1, np.int64)
-        np.cumsum([m["send_ids"].size for m in self.maps], out=self.send_off[1:])
+            sgn = self.kind != UNSIGNED
+            rsT, ciT, rsN, ciN = m["local"]
+            self.local.append(ogs.ogs_t().SetupMaps(m["N"], rsT, ciT, rsN if sgn else None,
+                                                    ciN if sgn else None, NrowsN=m["nlocalP"]))
+            rsT, ciT, rsN, ciN = m["halo"]
+            self.halo.append(ogs.ogs_t().SetupMaps(m["N"], rsT, ciT, rsN if sgn else None,
+                                                   ciN if sgn else None, NrowsN=m["nhaloP"]))
+            self.postT.append(ogs.ogs_t().SetupMaps(m["postT_cols"], *m["postT"]))
+            self.postN.append(ogs.ogs_t().SetupMaps(m["postN_cols"], *m["postN"]))
         dev = torch.device("cuda", torch.cuda.current_device())
-        self.d_send_ids = [torch.from_numpy(m["send_ids"]).to(dev) for m in self.maps]
-        recv_src = []
-        for j, m in enumerate(self.maps):
-            src = []
-            for r in range(self.R):
-                # position of (r -> j) entries inside r's send list
-                before = int(self.maps[r]["send_counts"][:j].sum())
-                cnt = int(self.maps[r]["send_counts"][j])
-                src.append(self.send_off[r] + before + np.arange(cnt))
-            recv_src.append(torch.from_numpy(np.concatenate(src).astype(np.int32)
-                                             if src else np.zeros(0, np.int32)).to(dev))
-        self.d_recv_src = recv_src
+        self.dev = dev
+        self.plan = {}
+        for which in ("T", "N"):
+            off = np.zeros(self.R + 1, np.int64)
+            np.cumsum([m["send_" + which].size for m in self.maps], out=off[1:])
+            send_ids = [torch.from_numpy(m["send_" + which]).to(dev) for m in self.maps]
+            recv_src = []
+            for j in range(self.R):
+                src = []
+                for r in range(self.R):
+                    cnts = self.maps[r]["send_counts_" + which]
+                    before = int(cnts[:j].sum())
+                    src.append(off[r] + before + np.arange(int(cnts[j])))
+                recv_src.append(torch.from_numpy(np.concatenate(src).astype(np.int32)).to(dev))
+            self.plan[which] = (off, send_ids, recv_src)
         self._bufs = {}
 
     def _buffers(self, dtype, k):
         import torch
         key = (dtype, k)
         if key not in self._bufs:
-            dev = self.d_send_ids[0].device if self.R else None
-            send = torch.empty(max(int(self.send_off[-1]) * k, 1), dtype=dtype, device=dev)
-            bufs = [torch.empty(max(m["post_cols"] * k, 1), dtype=dtype, device=dev) for m in self.maps]
+            nsend = max(int(self.plan["T"][0][-1]), 1)
+            send = torch.empty(nsend * k, dtype=dtype, device=self.dev)
+            bufs = [torch.empty(max(m["postT_cols"], m["postN_cols"], 1) * k, dtype=dtype, device=self.dev)
+                    for m in self.maps]
             self._bufs[key] = (send, bufs)
         return self._bufs[key]
 
-    def GatherScatterStart(self, vs, k, op, stream=None):
-        """Halo Gather, extract into the send buffers, exchange."""
+    # -- the halo steps (shared by ogs_t and halo_t) --
+    def _halo_start(self, vs, k, op, trans, stream):
+        which = "N" if int(trans) == int(ogs.NoTrans) else "T"
+        off, send_ids, recv_src = self.plan[which]
         send, bufs = self._buffers(vs[0].dtype, k)
         for r, m in enumerate(self.maps):
             nh = m["nhalo"]
             if nh:
-                self.halo[r].Gather(bufs[r][: nh * k], vs[r], k, op, ogs.Trans, stream=stream)
-            ns = m["send_ids"].size
+                self.halo[r].Gather(bufs[r][: nh * k], vs[r], k, op, trans, stream=stream)
+            ns = send_ids[r].numel()
             if ns:
-                ogs.extract(send[self.send_off[r] * k:(self.send_off[r] + ns) * k], bufs[r], self.d_send_ids[r],
-                            k, stream=stream)
+                ogs.extract(send[off[r] * k:(off[r] + ns) * k], bufs[r], send_ids[r], k, stream=stream)
         for j, m in enumerate(self.maps):
-            nrecv = self.d_recv_src[j].numel()
+            nrecv = recv_src[j].numel()
             if nrecv:
                 nh = m["nhalo"]
-                ogs.extract(bufs[j][nh * k:(nh + nrecv) * k], send, self.d_recv_src[j], k, stream=stream)
+                ogs.extract(bufs[j][nh * k:(nh + nrecv) * k], send, recv_src[j], k, stream=stream)
 
-    def GatherScatterFinish(self, vs, k, op, stream=None):
-        """Local GatherScatter, postmpi Gather (in place), halo Scatter."""
+    def _halo_finish(self, vs, k, op, trans, stream):
         _, bufs = self._buffers(vs[0].dtype, k)
+        notrans = int(trans) == int(ogs.NoTrans)
         for r, m in enumerate(self.maps):
-            if self.local[r].NlocalT:
-                self.local[r].GatherScatter(vs[r], k, op, ogs.Sym, stream=stream)
             nh = m["nhalo"]
-            if nh:
-                self.post[r].Gather(bufs[r][: nh * k], bufs[r][: m["post_cols"] * k], k, op, ogs.Trans,
-                                    stream=stream)
-                self.halo[r].Scatter(vs[r], bufs[r][: nh * k], k, ogs.Trans, stream=stream)
+            if not nh:
+                continue
+            post, cols = (self.postN[r], m["postN_cols"]) if notrans else (self.postT[r], m["postT_cols"])
+            post.Gather(bufs[r][: nh * k], bufs[r][: cols * k], k, op, ogs.Trans, stream=stream)
+            self.halo[r].Scatter(vs[r], bufs[r][: nh * k], k, trans, stream=stream)
 
-    def GatherScatter(self, vs, k, op=ogs.Add, stream=None):
-        self.GatherScatterStart(vs, k, op, stream)
-        self.GatherScatterFinish(vs, k, op, stream)
+    # -- ogs_t (ogs.cpp:39-123) --
+    def GatherScatterStart(self, vs, k, op=ogs.Add, trans=ogs.Sym, stream=None):
+        if self.kind == HALO:
+            raise ValueError("GatherScatter needs an Unsigned or Signed setup")
+        self._halo_start(vs, k, op, trans, stream)
+
+    def GatherScatterFinish(self, vs, k, op=ogs.Add, trans=ogs.Sym, stream=None):
+        for r in range(self.R):
+            if self.local[r].NlocalT:
+                self.local[r].GatherScatter(vs[r], k, op, trans, stream=stream)
+        self._halo_finish(vs, k, op, trans, stream)
+
+    def GatherScatter(self, vs, k, op=ogs.Add, trans=ogs.Sym, stream=None):
+        self.GatherScatterStart(vs, k, op, trans, stream)
+        self.GatherScatterFinish(vs, k, op, trans, stream)
+        return vs
+
+    # -- halo_t (ogsHalo.cpp:39-359, not gathered) --
+    def _need_halo(self):
+        if self.kind != HALO:
+            raise ValueError("Exchange and Combine need a Halo setup")
+
+    def ExchangeStart(self, vs, k, stream=None):
+        self._need_halo()
+        self._halo_start(vs, k, ogs.Add, ogs.NoTrans, stream)
+
+    def ExchangeFinish(self, vs, k, stream=None):
+        self._halo_finish(vs, k, ogs.Add, ogs.NoTrans, stream)
+
+    def Exchange(self, vs, k, stream=None):
+        self.ExchangeStart(vs, k, stream)
+        self.ExchangeFinish(vs, k, stream)
+        return vs
+
+    def CombineStart(self, vs, k, stream=None):
+        self._need_halo()
+        self._halo_start(vs, k, ogs.Add, ogs.Trans, stream)
+
+    def CombineFinish(self, vs, k, stream=None):
+        self._halo_finish(vs, k, ogs.Add, ogs.Trans, stream)
+
+    def Combine(self, vs, k, stream=None):
+        self.CombineStart(vs, k, stream)
+        self.CombineFinish(vs, k, stream)
         return vs
 
 
-__all__ = ["build_rank_maps", "ranks_ogs_t"]
+__all__ = ["build_rank_maps", "ranks_ogs_t", "UNSIGNED", "SIGNED", "HALO"]

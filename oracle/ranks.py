@@ -1,19 +1,25 @@
-"""Oracle for the emulated multi-rank GatherScatter (test infrastructure).
+"""Oracle for the emulated multi-rank gather-scatter (test infrastructure).
 
 Computes, from the global picture alone, what the reference's multi-rank
-Unsigned GatherScatter leaves on each rank (libs/ogs/ogs.cpp:39-123 with the
-all-to-all exchange of ogsAllToAll.cpp:126-175):
+GatherScatter (ogs_t, kinds Unsigned and Signed; libs/ogs/ogs.cpp:39-123 with
+the all-to-all exchange of ogsAllToAll.cpp:126-175) and halo_t
+Exchange/Combine (kind Halo; ogsHalo.cpp:39-359) leave on each rank:
 
-* an id held by one rank: that rank's ordinary fold over its members in
-  ascending local index (ogsOperator.cpp:311-360);
-* an id held by several ranks: each holder first folds its own members
-  (gatherHalo Gather, ogs.cpp:59), then folds, from the op identity, its own
-  partial followed by the other holders' partials in ascending rank (postmpi:
-  row h lists h first, then received entries in receive order, and entries
-  arrive ordered by source rank, ogsAllToAll.cpp:270-331), and writes that
-  to all its members (gatherHalo Scatter, ogs.cpp:120).  Holders of one id
-  can therefore differ in the last bit for floating-point Add and Mul, as in
-  the reference.
+* an id held by one rank (not for Halo, which leaves such ids alone): the
+  single-rank operation over that rank's members (ogsOperator.cpp:60-360);
+* an id held by several ranks: each holder folds its gather members -- N
+  members (positive ids) for NoTrans, all members otherwise -- into a partial
+  (gatherHalo Gather, ogs.cpp:59); it then folds, from the op identity, its own
+  partial (for NoTrans only if it has an N member) followed by the partials of
+  the other senders in ascending rank (for NoTrans only holders with an N
+  member send, ogsAllToAll.cpp:232-241; postmpi rows list the own entry, then
+  received entries in receive order, 270-331), and writes the result to its
+  N members (Trans) or all members (NoTrans, Sym) (gatherHalo Scatter,
+  ogs.cpp:120).  Holders of one id can therefore differ in the last bit for
+  floating-point Add and Mul, as in the reference.
+* N members: ids > 0 (Signed); all members on the rank holding the id's one
+  positive copy and none elsewhere (Halo, ogsSetup.cpp:790-800); all
+  (Unsigned).
 
 Every fold runs through the C oracle (OracleOgs), so the op semantics are the
 oracle's.  This module computes the expected fields; it builds no maps.
@@ -25,6 +31,12 @@ import numpy as np
 from . import OracleOgs
 
 
+def _identity(dtype, op):
+    dt = np.dtype(dtype)
+    big = np.finfo(dt).max if dt.kind == "f" else np.iinfo(dt).max
+    return {"add": dt.type(0), "mul": dt.type(1), "max": dt.type(-big), "min": dt.type(big)}[op]
+
+
 def _rows_by_first_appearance(ids):
     """Distinct nonzero |ids| in order of first appearance (the oracle's row order)."""
     a = np.abs(ids)
@@ -33,27 +45,46 @@ def _rows_by_first_appearance(ids):
     return u[np.argsort(first, kind="stable")]
 
 
-def ranks_gather_scatter(ids_list, vs, k, op):
-    """Expected fields after a multi-rank GatherScatter (Sym).  ids_list: int64
-    id arrays per rank; vs: numpy field arrays per rank (k interleaved
-    components, same dtype); op: "add" | "mul" | "max" | "min"."""
-    R = len(ids_list)
-    absids = [np.abs(np.asarray(x, dtype=np.int64)) for x in ids_list]
+def ranks_gather_scatter(ids_list, vs, k, op, kind="unsigned", trans="sym"):
+    """Expected fields after a multi-rank GatherScatter (kind "unsigned" or
+    "signed"), or a halo Exchange (kind "halo", op "add", trans "notrans") or
+    Combine (kind "halo", op "add", trans "trans").  ids_list: int64 id arrays
+    per rank; vs: numpy field arrays per rank (k interleaved components)."""
+    idsl = [np.asarray(x, dtype=np.int64) for x in ids_list]
+    absids = [np.abs(x) for x in idsl]
     holders = {}
     for r, a in enumerate(absids):
         for b in np.unique(a[a != 0]):
             holders.setdefault(int(b), []).append(r)
     shared = np.asarray(sorted(b for b, h in holders.items() if len(h) > 1), np.int64)
+    owner = {}
+    if kind == "halo":
+        for r, x in enumerate(idsl):
+            for b in np.unique(x[x > 0]):
+                owner[int(b)] = r
     dtype = vs[0].dtype
-    out, partial = [], []
+    notrans, tr = trans == "notrans", trans == "trans"
+
+    def nmask(r):
+        """N members of rank r."""
+        x, a = idsl[r], absids[r]
+        if kind == "unsigned":
+            return a != 0
+        if kind == "signed":
+            return x > 0
+        return np.array([owner.get(int(b), -1) == r for b in a], bool) & (a != 0)
+
+    out = [v.copy() for v in vs]
+    if kind != "halo":
+        for r, (x, a) in enumerate(zip(idsl, absids)):
+            loc = np.where(np.isin(a, shared), 0, x if kind == "signed" else a)
+            OracleOgs(loc, kind).gather_scatter(out[r], k, op, trans)
+    # partials of the shared ids: fold over the gather members
+    partial = []
     for r, a in enumerate(absids):
         sh = np.isin(a, shared)
-        x = vs[r].copy()
-        # local rows: ordinary single-rank fold, shared ids left out
-        OracleOgs(np.where(sh, 0, a), "unsigned").gather_scatter(x, k, op, "sym")
-        out.append(x)
-        # halo partials: Gather over the shared ids of this rank
-        ih = np.where(sh, a, 0)
+        gmem = sh & (nmask(r) if notrans else True)
+        ih = np.where(gmem, a, 0)
         rows = _rows_by_first_appearance(ih)
         p = {}
         if rows.size:
@@ -62,23 +93,31 @@ def ranks_gather_scatter(ids_list, vs, k, op):
             for i, b in enumerate(rows):
                 p[int(b)] = gv[i * k:(i + 1) * k]
         partial.append(p)
-    for r, a in enumerate(absids):
-        mine = [int(b) for b in _rows_by_first_appearance(np.where(np.isin(a, shared), a, 0))]
+    ident = np.full(k, _identity(dtype, op), dtype)
+    for j, a in enumerate(absids):
+        sh = np.isin(a, shared)
+        mine = [int(b) for b in _rows_by_first_appearance(np.where(sh, a, 0))]
         if not mine:
             continue
-        # each id's entries in fold order: own partial, then the other holders by rank
-        cid, vals = [], []
+        cid, vals, empty = [], [], set()
         for b in mine:
-            for s in [r] + [s for s in holders[b] if s != r]:
+            seq = ([j] if b in partial[j] else []) + [s for s in holders[b] if s != j and b in partial[s]]
+            if not seq:
+                empty.add(b)
+            for s in seq:
                 cid.append(b)
                 vals.append(partial[s][b])
-        cid = np.asarray(cid, np.int64)
-        w = np.concatenate(vals).astype(dtype)
-        gv = np.zeros(len(mine) * k, dtype)
-        OracleOgs(cid.copy(), "unsigned").gather(gv, w, k, op, "trans")
-        val = {b: gv[i * k:(i + 1) * k] for i, b in enumerate(mine)}
-        x = out[r]
-        for n in np.nonzero(np.isin(a, shared))[0]:
+        val = {b: ident for b in empty}
+        if cid:
+            uniq_order = [b for b in mine if b not in empty]
+            gv = np.zeros(len(uniq_order) * k, dtype)
+            OracleOgs(np.asarray(cid, np.int64), "unsigned").gather(gv, np.concatenate(vals).astype(dtype), k, op,
+                                                                    "trans")
+            for i, b in enumerate(uniq_order):
+                val[b] = gv[i * k:(i + 1) * k]
+        smem = sh & (nmask(j) if tr else True)
+        x = out[j]
+        for n in np.nonzero(smem)[0]:
             x[n * k:(n + 1) * k] = val[int(a[n])]
     return out
 
@@ -99,3 +138,27 @@ def partition_box(nx, ny, nz, p, R, how="slabs", seed=0):
         owner = (mesh.splitmix64(np.arange(ne, dtype=np.uint64) + np.uint64(seed)) % np.uint64(R)).astype(np.int64)
     el = ids.reshape(ne, npe)
     return [el[owner == r].reshape(-1).copy() for r in range(R)]
+
+
+def signed_parts(parts, seed, kind):
+    """Signs for a partition.  "signed": each entry negative with probability
+    1/2 (a seeded generator).  "halo": each id's one positive copy on the
+    lowest rank holding it, at its first local occurrence there, every other
+    copy negative (ogsSetup.cpp:293-296 needs exactly one)."""
+    from dawgs_gb300 import mesh
+    out = []
+    if kind == "signed":
+        for r, p in enumerate(parts):
+            flip = (mesh.splitmix64(np.arange(p.size, dtype=np.uint64) + np.uint64(seed + 1000 * r)) & np.uint64(1))
+            out.append(np.where(flip.astype(bool), -p, p))
+        return out
+    seen = set()
+    for p in parts:
+        q = -np.abs(p)
+        for n in range(p.size):
+            b = int(abs(p[n]))
+            if b and b not in seen:
+                seen.add(b)
+                q[n] = b
+        out.append(q)
+    return out

@@ -51,6 +51,36 @@ def test_ranks_match_oracle(setups, oracle_mod, key, dtype, op):
             assert same_bits(np.concatenate([d.cpu().numpy() for d in ds]), single)
 
 
+MODES = [("signed", "sym", "add"), ("signed", "notrans", "add"), ("signed", "trans", "mul"),
+         ("signed", "notrans", "max"), ("halo", "notrans", "add"), ("halo", "trans", "add")]
+_T = {"sym": ogs.Sym, "notrans": ogs.NoTrans, "trans": ogs.Trans}
+
+
+@pytest.mark.parametrize("key", PARTS[:4], ids=lambda p: f"{p[0]}-{p[1]}-{p[2]}")
+@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int64], ids=lambda t: np.dtype(t).name)
+@pytest.mark.parametrize("kind,trans,op", MODES)
+def test_signed_and_halo_ranks_match_oracle(cuda, oracle_mod, key, dtype, kind, trans, op):
+    """ogs_t GatherScatter on Signed ranks and halo_t Exchange (NoTrans) /
+    Combine (Trans) on Halo ranks."""
+    box, R, how = key
+    parts = oranks.signed_parts(oranks.partition_box(*box, R, how=how, seed=17), 5, kind)
+    rk = ranks.ranks_ogs_t(parts, ranks.SIGNED if kind == "signed" else ranks.HALO)
+    for k in (1, 2):
+        vs = [values(k * p.size, dtype, op, seed=70 + i + 3 * k) for i, p in enumerate(parts)]
+        want = oranks.ranks_gather_scatter(parts, vs, k, op, kind, trans)
+        ds = [torch.from_numpy(v.copy()).cuda() for v in vs]
+        if kind == "signed":
+            rk.GatherScatter(ds, k, ogs.Op[op.capitalize()], _T[trans])
+        elif trans == "notrans":
+            rk.Exchange(ds, k)
+        else:
+            rk.Combine(ds, k)
+        torch.cuda.synchronize()
+        for r, (d, w) in enumerate(zip(ds, want)):
+            got = d.cpu().numpy()
+            assert same_bits(got, w), (key, kind, trans, k, r, first_diff(got, w))
+
+
 def test_ranks_float_add_close_to_single_rank(setups, oracle_mod):
     parts, rk = setups[((5, 4, 4, 2), 4, "random")]
     vs = [values(p.size, np.float64, "add", seed=3 + i) for i, p in enumerate(parts)]
@@ -98,3 +128,18 @@ def test_operator_with_shared_column_refuses_writes(cuda):
         g.GatherScatter(v, 1, ogs.Add, ogs.Sym)
     with pytest.raises(ogs.OgsError):
         g.Scatter(v, gv, 1, ogs.Trans)
+
+
+@pytest.mark.parametrize("op,ident", [("add", 0.0), ("max", -np.finfo(np.float64).max)])
+def test_operator_empty_rows_gather_identity(cuda, op, ident):
+    g = ogs.ogs_t().SetupMaps(4, [0, 2, 2, 3, 3], [0, 2, 1])  # rows 1 and 3 empty
+    v = torch.tensor([1.0, 2.0, 3.0, 4.0], dtype=torch.float64, device="cuda")
+    gv = torch.full((4,), 7.0, dtype=torch.float64, device="cuda")
+    g.Gather(gv, v, 1, ogs.Op[op.capitalize()], ogs.Trans)
+    torch.cuda.synchronize()
+    first = 4.0 if op == "add" else 3.0
+    assert gv.cpu().tolist() == [first, ident, 2.0, ident]
+    g.GatherScatter(v, 1, ogs.Op[op.capitalize()], ogs.Sym)  # empty rows write nothing
+    torch.cuda.synchronize()
+    assert v.cpu().tolist() == [first, 2.0, first, 4.0]
+

@@ -32,60 +32,101 @@ def _fold(vals, op, dt):
     return a
 
 
-def _gather(rs, ci, src, k, op, dt):
-    out = np.zeros((len(rs) - 1) * k, dt)
-    for r in range(len(rs) - 1):
-        for c in range(k):
-            out[r * k + c] = _fold([src[m * k + c] for m in ci[rs[r]:rs[r + 1]]], op, dt)
+def _fold_rows(rs, ci, rows, src, k, op, dt):
+    out = {}
+    for r in rows:
+        out[r] = np.array([_fold([src[m * k + c] for m in ci[rs[r]:rs[r + 1]]], op, dt) for c in range(k)], dt)
     return out
 
 
-def _scatter(rs, ci, dst, gv, k):
-    for r in range(len(rs) - 1):
+def _op_gather(maps4, nrowsN, src, gv, k, op, dt, trans):
+    """ogsOperator Gather (ogsOperator.cpp:60-97): NoTrans folds the N members
+    of rows < NrowsN, otherwise the T members of every row."""
+    rsT, ciT, rsN, ciN = maps4
+    rs, ci, rows = (rsN, ciN, range(nrowsN)) if trans == "notrans" else (rsT, ciT, range(len(rsT) - 1))
+    for r, val in _fold_rows(rs, ci, rows, src, k, op, dt).items():
+        gv[r * k:(r + 1) * k] = val
+
+
+def _op_scatter(maps4, nrowsN, dst, gv, k, trans):
+    """ogsOperator Scatter (ogsOperator.cpp:206-238): Trans writes the N
+    members of rows < NrowsN, otherwise the T members of every row."""
+    rsT, ciT, rsN, ciN = maps4
+    rs, ci, rows = (rsN, ciN, range(nrowsN)) if trans == "trans" else (rsT, ciT, range(len(rsT) - 1))
+    for r in rows:
         for m in ci[rs[r]:rs[r + 1]]:
             dst[m * k:(m + 1) * k] = gv[r * k:(r + 1) * k]
 
 
-def cpu_emulate(maps, vs, k, op):
+def _op_gs(maps4, v, k, op, dt, trans):
+    """ogsOperator GatherScatter (ogsOperator.cpp:311-360): gather N members
+    for NoTrans, T otherwise; write N members for Trans, T otherwise; every row."""
+    rsT, ciT, rsN, ciN = maps4
+    g = (rsN, ciN) if trans == "notrans" else (rsT, ciT)
+    s = (rsN, ciN) if trans == "trans" else (rsT, ciT)
+    vals = _fold_rows(*g, range(len(rsT) - 1), v, k, op, dt)
+    for r, val in vals.items():
+        for m in s[1][s[0][r]:s[0][r + 1]]:
+            v[m * k:(m + 1) * k] = val
+
+
+def cpu_emulate(maps, vs, k, op, trans="sym", halo_only=False):
+    """The reference's multi-rank steps over the emulated maps, one scalar at a time."""
     dt = vs[0].dtype
     R = len(maps)
+    which = "N" if trans == "notrans" else "T"
     vs = [v.copy() for v in vs]
     bufs, sends = [], []
     for m, v in zip(maps, vs):
-        hb = np.zeros(m["post_cols"] * k, dt)
-        hb[: m["nhalo"] * k] = _gather(*m["halo"], v, k, op, dt)
+        hb = np.zeros(max(m["postT_cols"], m["postN_cols"]) * k, dt)
+        _op_gather(m["halo"], m["nhaloP"], v, hb, k, op, dt, trans)
         bufs.append(hb)
-        sends.append(np.concatenate([hb[h * k:(h + 1) * k] for h in m["send_ids"]]) if m["send_ids"].size
-                     else np.zeros(0, dt))
+        ids = m["send_" + which]
+        sends.append(np.concatenate([hb[h * k:(h + 1) * k] for h in ids]) if ids.size else np.zeros(0, dt))
     for j, m in enumerate(maps):
         parts = []
         for r in range(R):
-            before = int(maps[r]["send_counts"][:j].sum()) * k
-            parts.append(sends[r][before:before + int(maps[r]["send_counts"][j]) * k])
-        recv = np.concatenate(parts) if parts else np.zeros(0, dt)
-        bufs[j][m["nhalo"] * k:] = recv
+            cnt = maps[r]["send_counts_" + which]
+            before = int(cnt[:j].sum()) * k
+            parts.append(sends[r][before:before + int(cnt[j]) * k])
+        recv = np.concatenate(parts)
+        bufs[j][m["nhalo"] * k:m["nhalo"] * k + recv.size] = recv
     for m, v, hb in zip(maps, vs, bufs):
-        rs, ci = m["local"]
-        _scatter(rs, ci, v, _gather(rs, ci, v, k, op, dt), k)
-        hb[: m["nhalo"] * k] = _gather(*m["post"], hb, k, op, dt)
-        _scatter(*m["halo"], v, hb[: m["nhalo"] * k], k)
+        if not halo_only:
+            _op_gs(m["local"], v, k, op, dt, trans)
+        nh = m["nhalo"]
+        post = m["post" + which]
+        out = hb.copy()
+        for r, val in _fold_rows(*post, range(nh), hb, k, op, dt).items():
+            out[r * k:(r + 1) * k] = val
+        _op_scatter(m["halo"], m["nhaloP"], v, out[: nh * k], k, trans)
     return vs
 
 
 CASES = [((4, 3, 2, 2), 2, "slabs"), ((4, 3, 2, 2), 3, "random"), ((3, 3, 3, 1), 4, "random"),
          ((5, 2, 2, 2), 5, "slabs")]
+KINDS = {"unsigned": ranks.UNSIGNED, "signed": ranks.SIGNED, "halo": ranks.HALO}
+
+
+# (kind, transpose, op): ogs_t GatherScatter for Unsigned/Signed; halo_t
+# Exchange (NoTrans) and Combine (Trans) always add
+MODES = [("unsigned", "sym", "add"), ("unsigned", "sym", "max"), ("signed", "sym", "add"),
+         ("signed", "notrans", "add"), ("signed", "trans", "max"), ("signed", "notrans", "min"),
+         ("halo", "notrans", "add"), ("halo", "trans", "add")]
 
 
 @pytest.mark.parametrize("box,R,how", CASES)
 @pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int32], ids=lambda t: np.dtype(t).name)
-@pytest.mark.parametrize("op", ["add", "max"])
-def test_emulated_ranks_match_oracle(oracle_mod, box, R, how, dtype, op):
+@pytest.mark.parametrize("kind,trans,op", MODES)
+def test_emulated_ranks_match_oracle(oracle_mod, box, R, how, dtype, kind, trans, op):
     parts = oranks.partition_box(*box, R, how=how, seed=9)
-    maps = ranks.build_rank_maps(parts)
+    if kind != "unsigned":
+        parts = oranks.signed_parts(parts, 4, kind)
+    maps = ranks.build_rank_maps(parts, KINDS[kind])
     for k in (1, 2):
         vs = [values(k * p.size, dtype, op, seed=20 + i) for i, p in enumerate(parts)]
-        got = cpu_emulate(maps, vs, k, op)
-        want = oranks.ranks_gather_scatter(parts, vs, k, op)
+        got = cpu_emulate(maps, vs, k, op, trans, halo_only=kind == "halo")
+        want = oranks.ranks_gather_scatter(parts, vs, k, op, kind, trans)
         for g, w in zip(got, want):
             assert g.tobytes() == w.tobytes(), (box, R, how, k)
 
@@ -96,16 +137,33 @@ def test_maps_are_consistent():
     for j, m in enumerate(maps):
         # every halo row receives one entry from every other holder of its id
         holders = sum(np.isin(m["halo_ids"], np.abs(p)).astype(int) for i, p in enumerate(parts) if i != j)
-        assert np.array_equal(np.bincount(m["recv_rows"], minlength=m["nhalo"]), holders)
-        assert int(m["recv_counts"].sum()) == m["recv_rows"].size
-        assert sum(int(maps[r]["send_counts"][j]) for r in range(len(maps))) == m["recv_rows"].size
+        assert np.array_equal(np.bincount(m["recv_rows_T"], minlength=m["nhalo"]), holders)
+        assert sum(int(maps[r]["send_counts_T"][j]) for r in range(len(maps))) == m["recv_rows_T"].size
         # every local node is in exactly one local or halo row
         cols = np.concatenate([m["local"][1], m["halo"][1]])
         assert np.array_equal(np.sort(cols), np.arange(m["N"]))
         # the library accepts each operator's maps (host-only handles)
-        for N, (rs, ci) in ((m["N"], m["local"]), (m["N"], m["halo"]), (m["post_cols"], m["post"])):
-            g = ogs.ogs_t().SetupMaps(N, rs, ci, host_only=True)
-            assert g.NlocalT == rs.size - 1 and g.nnzT == ci.size
+        for N, maps4 in ((m["N"], m["local"]), (m["N"], m["halo"])):
+            g = ogs.ogs_t().SetupMaps(N, *maps4[:2], host_only=True)
+            assert g.NlocalT == maps4[0].size - 1 and g.nnzT == maps4[1].size
+        for N, (rs, ci) in ((m["postT_cols"], m["postT"]), (m["postN_cols"], m["postN"])):
+            ogs.ogs_t().SetupMaps(N, rs, ci, host_only=True)
+
+
+def test_signed_and_halo_maps_accepted():
+    parts = oranks.partition_box(5, 4, 3, 2, 3, how="random", seed=8)
+    for kind in ("signed", "halo"):
+        sp = oranks.signed_parts(parts, 2, kind)
+        for m in ranks.build_rank_maps(sp, KINDS[kind]):
+            for N, maps4, nP in ((m["N"], m["local"], m["nlocalP"]), (m["N"], m["halo"], m["nhaloP"])):
+                g = ogs.ogs_t().SetupMaps(N, maps4[0], maps4[1], maps4[2], maps4[3], NrowsN=nP, host_only=True)
+                assert g.NlocalP == nP and g.nnzN == maps4[3].size
+
+
+def test_halo_needs_one_positive_copy():
+    parts = oranks.partition_box(3, 2, 2, 1, 2, how="slabs")
+    with pytest.raises(ValueError):
+        ranks.build_rank_maps(parts, ranks.HALO)  # every copy positive
 
 
 def test_setup_maps_rejects_bad_maps(built_lib):
@@ -136,3 +194,14 @@ def test_setup_maps_rejects_bad_maps(built_lib):
     assert b"NrowsN" in built_lib.ogs_last_error_string()
     assert setup(4, [0, 2, 4], [0, 1, 2, 3], [0, 1, 1], [1], NrowsN=1) == _lib.OGS_OK
     built_lib.ogs_free(h)
+
+
+def test_setup_maps_with_empty_rows():
+    """Rows without members (postmpi N rows with nothing received) are valid:
+    they go to the general bucket."""
+    rs = np.array([0, 2, 2, 3, 3, 3], np.int32)  # rows 1, 3 and 4 empty
+    ci = np.array([0, 2, 1], np.int32)
+    g = ogs.ogs_t().SetupMaps(4, rs, ci, host_only=True)
+    st = g.layout_stats()
+    assert g.NlocalT == 5 and st["rows_general"] == 3
+
