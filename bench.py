@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--batch-meshes", type=int, default=256)
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-refdev", action="store_true")
+    ap.add_argument("--no-partitioned", action="store_true")
     ap.add_argument("--served-requests", type=int, default=100000)
     ap.add_argument("--sweep", action="store_true",
                     help="print the results tables (one JSON line per case) instead of the bench line")
@@ -324,6 +325,63 @@ def run_served(a, dev, L, stream):
             "speedup_vs_plain": sat["dofs_per_s"] / (dofs_plain / t_plain)}
 
 
+def run_partitioned(a, dev, stream, single_step_s, ranks_n=8):
+    """The benchmark mesh split into `ranks_n` slabs of elements (z-major
+    element order, like MakeIds' rank grid along z), run as emulated ranks on
+    this GPU: per rank a halo Gather, send-buffer packing, the exchange as a
+    device gather, the local GatherScatter, the postmpi Gather and the halo
+    Scatter (dawgs_gb300/ranks.py).  The whole sequence of every rank is one
+    CUDA graph; each step restores the fields and flushes L2 first."""
+    import torch
+    from dawgs_gb300 import mesh, ogs, ranks
+    ids = mesh.box_ids(a.nx, a.ny, a.nz, a.p)
+    ne, npe = a.nx * a.ny * a.nz, (a.p + 1) ** 3
+    owner = (np.arange(ne) * ranks_n) // ne
+    parts = [ids.reshape(ne, npe)[owner == r].reshape(-1).copy() for r in range(ranks_n)]
+    t0 = time.perf_counter()
+    rk = ranks.ranks_ogs_t(parts)
+    setup_s = time.perf_counter() - t0
+    pristine = [torch.from_numpy(mesh.uniform_values(p.size, np.float64, -1.0, 1.0, seed=100 + r)).to(dev)
+                for r, p in enumerate(parts)]
+    vs = [x.clone() for x in pristine]
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(side):
+        for _ in range(3):
+            rk.GatherScatter(vs, 1, ogs.Add)
+    torch.cuda.current_stream(dev).wait_stream(side)
+    torch.cuda.synchronize(dev)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        rk.GatherScatter(vs, 1, ogs.Add)
+    l2 = torch.cuda.get_device_properties(dev).L2_cache_size
+    flush = torch.empty(2 * l2 // 4 + 1, dtype=torch.float32, device=dev)
+    sink = torch.empty((), dtype=torch.float32, device=dev)
+    ts = []
+    for it in range(a.warmup + a.steps):
+        for v, p0 in zip(vs, pristine):
+            v.copy_(p0)
+        flush.zero_()
+        torch.sum(flush, dim=0, out=sink)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        graph.replay()
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        if it >= a.warmup:
+            ts.append(e0.elapsed_time(e1) * 1e-3)
+    t = sum(ts) / len(ts)
+    nglobal = (a.nx * a.p + 1) * (a.ny * a.p + 1) * (a.nz * a.p + 1)
+    halo_rows = sum(m["nhalo"] for m in rk.maps)
+    sent = int(sum(m["send_T"].size for m in rk.maps))
+    return {"workload": f"{workload_name(a)}, elements split into {ranks_n} z-slabs, emulated ranks on one GPU",
+            "ranks": ranks_n, "ms_per_step": t * 1e3, "value": nglobal / t, "unit": "DOFS/s",
+            "single_rank_ms_per_step": single_step_s * 1e3, "overhead_vs_single_rank": t / single_step_s,
+            "halo_rows": int(halo_rows), "exchanged_entries": sent, "setup_s": setup_s,
+            "graph": "all ranks' launches replayed from one CUDA graph",
+            "l2": "flushed between steps"}
+
+
 def aggregate_over_ranks(seconds, units, device=None):
     """Replicas: the job's time is the slowest rank's, its work the sum of all
     ranks' units.  Returns (seconds, units, throughput)."""
@@ -523,6 +581,10 @@ def run_ours(a):
     if rank == 0 and world == 1 and not a.no_served:
         served = run_served(a, dev, L, stream)
 
+    partitioned = None
+    if rank == 0 and world == 1 and not a.no_partitioned and a.k == 1 and a.dtype == "float64" and a.op == "add":
+        partitioned = run_partitioned(a, dev, stream, per_step)
+
     peak, peak_src = hbm_peak()
     nbytes_alg = alg_bytes(ids.size, g.nnzT, g.NlocalT, a.k, s)
     achieved = nbytes_alg / per_step / 1e9
@@ -551,6 +613,7 @@ def run_ours(a):
         "served": served,
         "setup": setup_s,
         "reference_device_equivalent": refdev_line,
+        "partitioned": partitioned,
         "gpu_launches": a.steps,
         "clocks": clk.summary(),
         "wall_ms_per_step_incl_restore_and_flush": 1e3 * (w1 - w0) / a.steps,

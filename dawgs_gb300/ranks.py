@@ -55,6 +55,15 @@ from . import ogs
 UNSIGNED, SIGNED, HALO = int(ogs.Unsigned), int(ogs.Signed), int(ogs.Halo)
 
 
+def _distinct(x):
+    """Sorted distinct values (sort-based: faster than np.unique's hash path
+    on millions of ids)."""
+    s = np.sort(x)
+    if s.size == 0:
+        return s
+    return s[np.concatenate(([True], s[1:] != s[:-1]))]
+
+
 def _csr(rows_of_members, nrows, keep=None):
     """CSR map with members of each row in ascending local index:
     rows_of_members[n] = row of local node n, or -1; keep: optional mask."""
@@ -94,14 +103,15 @@ def build_rank_maps(ids_list, kind=UNSIGNED):
     R = len(ids_list)
     ids_list = [np.asarray(x, dtype=np.int64) for x in ids_list]
     absids = [np.abs(x) for x in ids_list]
-    per_rank = [np.unique(a[a != 0]) for a in absids]
+    per_rank = [_distinct(a[a != 0]) for a in absids]
     allids = np.concatenate(per_rank) if per_rank else np.zeros(0, np.int64)
     ids_u, nranks = np.unique(allids, return_counts=True)
     shared_ids = ids_u[nranks > 1]
     if kind == HALO:
         # every id group needs exactly one positive id over all ranks (ogsSetup.cpp:293-296)
         pos_all = np.concatenate([x[x > 0] for x in ids_list]) if R else np.zeros(0, np.int64)
-        u, c = np.unique(pos_all, return_counts=True)
+        u = _distinct(pos_all)
+        c = np.searchsorted(np.sort(pos_all), u, side="right") - np.searchsorted(np.sort(pos_all), u, side="left")
         cnt = np.zeros(ids_u.size, np.int64)
         cnt[np.searchsorted(ids_u, u)] = c
         bad = ids_u[cnt != 1]
@@ -120,7 +130,7 @@ def build_rank_maps(ids_list, kind=UNSIGNED):
         if kind == UNSIGNED:
             has_pos[:] = True
         else:
-            has_pos[np.unique(node_uniq[nz][x[nz] > 0])] = True
+            has_pos[node_uniq[nz][x[nz] > 0]] = True
         loc_p, loc_n = _number_rows(first, has_pos, np.nonzero(~is_sh)[0])
         hal_p, hal_n = _number_rows(first, has_pos, np.nonzero(is_sh)[0])
         if kind == HALO:
@@ -155,37 +165,44 @@ def build_rank_maps(ids_list, kind=UNSIGNED):
                     "halo_ids": uniq[order_h], "halo_pos": has_pos[order_h]})
     # exchange: rank r sends halo row h (id b) to every other holder j,
     # ordered by (j, h); N sends are the rows with a positive member
-    holders = {}
-    for r, m in enumerate(out):
-        for h, b in enumerate(m["halo_ids"]):
-            holders.setdefault(int(b), []).append((r, h, bool(m["halo_pos"][h])))
-    sends = [[[] for _ in range(R)] for _ in range(R)]  # sends[r][j] = [(h_r, h_j, positive on r)]
-    for lst in holders.values():
-        for r, hr, pr in lst:
-            for j, hj, _ in lst:
-                if j != r:
-                    sends[r][j].append((hr, hj, pr))
+    B = np.concatenate([m["halo_ids"] for m in out]) if R else np.zeros(0, np.int64)
+    RK = np.concatenate([np.full(m["nhalo"], r, np.int64) for r, m in enumerate(out)]) if R else B
+    H = np.concatenate([np.arange(m["nhalo"]) for m in out]) if R else B
+    P = np.concatenate([m["halo_pos"] for m in out]) if R else np.zeros(0, bool)
+    o = np.lexsort((RK, B))
+    B, RK, H, P = B[o], RK[o], H[o], P[o]
+    n = B.size
+    newgrp = np.ones(n, bool)
+    newgrp[1:] = B[1:] != B[:-1]
+    gid = np.cumsum(newgrp) - 1
+    gstart = np.nonzero(newgrp)[0]
+    gsize = np.diff(np.append(gstart, n))
+    per = gsize[gid]                                   # group size of each holder entry
+    i_idx = np.repeat(np.arange(n), per)               # every (holder, holder) pair of a group
+    base = np.repeat(np.cumsum(per) - per, per)
+    j_idx = gstart[gid[i_idx]] + (np.arange(i_idx.size) - base)
+    keep = i_idx != j_idx
+    i_idx, j_idx = i_idx[keep], j_idx[keep]
+    src, dst, hs, hd, ps = RK[i_idx], RK[j_idx], H[i_idx], H[j_idx], P[i_idx]
+    so = np.lexsort((hs, dst, src))                    # send order: source, destination, source row
     for r in range(R):
-        sT, sN, cT, cN = [], [], [], []
-        for j in range(R):
-            sends[r][j].sort()
-            sT += [hr for hr, _, _ in sends[r][j]]
-            sN += [hr for hr, _, p in sends[r][j] if p]
-            cT.append(len(sends[r][j]))
-            cN.append(sum(1 for _, _, p in sends[r][j] if p))
+        sel = so[src[so] == r]
         m = out[r]
-        m["send_T"], m["send_N"] = np.asarray(sT, np.int32), np.asarray(sN, np.int32)
-        m["send_counts_T"], m["send_counts_N"] = np.asarray(cT, np.int64), np.asarray(cN, np.int64)
+        m["send_T"] = hs[sel].astype(np.int32)
+        m["send_N"] = hs[sel][ps[sel]].astype(np.int32)
+        m["send_counts_T"] = np.bincount(dst[sel], minlength=R).astype(np.int64)
+        m["send_counts_N"] = np.bincount(dst[sel][ps[sel]], minlength=R).astype(np.int64)
+    ro = np.lexsort((hs, src, dst))                    # receive order: destination, source, source row
     for j in range(R):
+        sel = ro[dst[ro] == j]
         m = out[j]
-        rT = [hj for r in range(R) for _, hj, _ in sends[r][j]]
-        rN = [hj for r in range(R) for _, hj, p in sends[r][j] if p]
-        m["recv_rows_T"], m["recv_rows_N"] = np.asarray(rT, np.int64), np.asarray(rN, np.int64)
+        m["recv_rows_T"] = hd[sel].astype(np.int64)
+        m["recv_rows_N"] = hd[sel][ps[sel]].astype(np.int64)
         nh, nhp = m["nhalo"], m["nhaloP"]
         m["postT"] = _csr(np.concatenate([np.arange(nh), m["recv_rows_T"]]), nh)
         m["postN"] = _csr(np.concatenate([np.arange(nhp), np.full(nh - nhp, -1), m["recv_rows_N"]]), nh)
-        m["postT_cols"] = nh + len(rT)
-        m["postN_cols"] = nh + len(rN)
+        m["postT_cols"] = nh + m["recv_rows_T"].size
+        m["postN_cols"] = nh + m["recv_rows_N"].size
     return out
 
 
@@ -241,50 +258,126 @@ class ranks_ogs_t:
             self._bufs[key] = (send, bufs)
         return self._bufs[key]
 
-    # -- the halo steps (shared by ogs_t and halo_t) --
-    def _halo_start(self, vs, k, op, trans, stream):
-        which = "N" if int(trans) == int(ogs.NoTrans) else "T"
-        off, send_ids, recv_src = self.plan[which]
+    # -- the steps; every rank runs on its own stream, forked from and joined
+    # back to the caller's stream, so the ranks' small launches overlap --
+    def _streams(self):
+        import torch
+        if not hasattr(self, "_rank_streams"):
+            self._rank_streams = [torch.cuda.Stream(self.dev) for _ in range(self.R)]
+        return self._rank_streams
+
+    def _fork(self, stream):
+        import torch
+        main = stream if stream is not None else torch.cuda.current_stream(self.dev)
+        ev = torch.cuda.Event()
+        ev.record(main)
+        for s in self._streams():
+            s.wait_event(ev)
+        return main
+
+    def _join(self, main):
+        import torch
+        for s in self._streams():
+            ev = torch.cuda.Event()
+            ev.record(s)
+            main.wait_event(ev)
+
+    def _sends(self, vs, k, op, trans, which):
+        """Halo Gather and send packing on every rank's stream; returns one
+        event per rank."""
+        import torch
+        off, send_ids, _ = self.plan[which]
         send, bufs = self._buffers(vs[0].dtype, k)
-        for r, m in enumerate(self.maps):
+        done = []
+        for r, (m, s) in enumerate(zip(self.maps, self._streams())):
             nh = m["nhalo"]
             if nh:
-                self.halo[r].Gather(bufs[r][: nh * k], vs[r], k, op, trans, stream=stream)
+                self.halo[r].Gather(bufs[r][: nh * k], vs[r], k, op, trans, stream=s)
             ns = send_ids[r].numel()
             if ns:
-                ogs.extract(send[off[r] * k:(off[r] + ns) * k], bufs[r], send_ids[r], k, stream=stream)
-        for j, m in enumerate(self.maps):
-            nrecv = recv_src[j].numel()
-            if nrecv:
-                nh = m["nhalo"]
-                ogs.extract(bufs[j][nh * k:(nh + nrecv) * k], send, recv_src[j], k, stream=stream)
+                ogs.extract(send[off[r] * k:(off[r] + ns) * k], bufs[r], send_ids[r], k, stream=s)
+            ev = torch.cuda.Event()
+            ev.record(s)
+            done.append(ev)
+        return done
 
-    def _halo_finish(self, vs, k, op, trans, stream):
+    def _recv(self, j, k, which, sent, s, dtype):
+        """Rank j's receive region, once every rank's send buffer is packed."""
+        _, _, recv_src = self.plan[which]
+        send, bufs = self._buffers(dtype, k)
+        for ev in sent:
+            s.wait_event(ev)
+        nrecv = recv_src[j].numel()
+        if nrecv:
+            nh = self.maps[j]["nhalo"]
+            ogs.extract(bufs[j][nh * k:(nh + nrecv) * k], send, recv_src[j], k, stream=s)
+
+    def _post_scatter(self, j, vs, k, op, trans, which, s):
         _, bufs = self._buffers(vs[0].dtype, k)
-        notrans = int(trans) == int(ogs.NoTrans)
-        for r, m in enumerate(self.maps):
-            nh = m["nhalo"]
-            if not nh:
-                continue
-            post, cols = (self.postN[r], m["postN_cols"]) if notrans else (self.postT[r], m["postT_cols"])
-            post.Gather(bufs[r][: nh * k], bufs[r][: cols * k], k, op, ogs.Trans, stream=stream)
-            self.halo[r].Scatter(vs[r], bufs[r][: nh * k], k, trans, stream=stream)
+        m = self.maps[j]
+        nh = m["nhalo"]
+        if not nh:
+            return
+        post, cols = (self.postN[j], m["postN_cols"]) if which == "N" else (self.postT[j], m["postT_cols"])
+        post.Gather(bufs[j][: nh * k], bufs[j][: cols * k], k, op, ogs.Trans, stream=s)
+        self.halo[j].Scatter(vs[j], bufs[j][: nh * k], k, trans, stream=s)
+
+    def _local(self, vs, k, op, trans):
+        for r, s in enumerate(self._streams()):
+            if self.local[r].NlocalT:
+                self.local[r].GatherScatter(vs[r], k, op, trans, stream=s)
+
+    def _which(self, trans):
+        return "N" if int(trans) == int(ogs.NoTrans) else "T"
+
+    def _start(self, vs, k, op, trans, stream):
+        which = self._which(trans)
+        main = self._fork(stream)
+        sent = self._sends(vs, k, op, trans, which)
+        for j, s in enumerate(self._streams()):
+            self._recv(j, k, which, sent, s, vs[0].dtype)
+        self._join(main)
+
+    def _finish(self, vs, k, op, trans, stream, local):
+        which = self._which(trans)
+        main = self._fork(stream)
+        if local:
+            self._local(vs, k, op, trans)
+        for j, s in enumerate(self._streams()):
+            self._post_scatter(j, vs, k, op, trans, which, s)
+        self._join(main)
+
+    def _whole(self, vs, k, op, trans, stream, local):
+        """Start and Finish in one pass: each rank's local GatherScatter runs
+        while the other ranks still pack their sends (the overlap the
+        reference's Start/Finish split is for)."""
+        which = self._which(trans)
+        main = self._fork(stream)
+        sent = self._sends(vs, k, op, trans, which)
+        if local:
+            self._local(vs, k, op, trans)
+        for j, s in enumerate(self._streams()):
+            self._recv(j, k, which, sent, s, vs[0].dtype)
+            self._post_scatter(j, vs, k, op, trans, which, s)
+        self._join(main)
 
     # -- ogs_t (ogs.cpp:39-123) --
-    def GatherScatterStart(self, vs, k, op=ogs.Add, trans=ogs.Sym, stream=None):
+    def _need_gs(self):
         if self.kind == HALO:
             raise ValueError("GatherScatter needs an Unsigned or Signed setup")
-        self._halo_start(vs, k, op, trans, stream)
+
+    def GatherScatterStart(self, vs, k, op=ogs.Add, trans=ogs.Sym, stream=None):
+        """Halo Gather, send packing, exchange."""
+        self._need_gs()
+        self._start(vs, k, op, trans, stream)
 
     def GatherScatterFinish(self, vs, k, op=ogs.Add, trans=ogs.Sym, stream=None):
-        for r in range(self.R):
-            if self.local[r].NlocalT:
-                self.local[r].GatherScatter(vs[r], k, op, trans, stream=stream)
-        self._halo_finish(vs, k, op, trans, stream)
+        """Local GatherScatter, postmpi Gather, halo Scatter."""
+        self._finish(vs, k, op, trans, stream, local=True)
 
     def GatherScatter(self, vs, k, op=ogs.Add, trans=ogs.Sym, stream=None):
-        self.GatherScatterStart(vs, k, op, trans, stream)
-        self.GatherScatterFinish(vs, k, op, trans, stream)
+        self._need_gs()
+        self._whole(vs, k, op, trans, stream, local=True)
         return vs
 
     # -- halo_t (ogsHalo.cpp:39-359, not gathered) --
@@ -294,26 +387,26 @@ class ranks_ogs_t:
 
     def ExchangeStart(self, vs, k, stream=None):
         self._need_halo()
-        self._halo_start(vs, k, ogs.Add, ogs.NoTrans, stream)
+        self._start(vs, k, ogs.Add, ogs.NoTrans, stream)
 
     def ExchangeFinish(self, vs, k, stream=None):
-        self._halo_finish(vs, k, ogs.Add, ogs.NoTrans, stream)
+        self._finish(vs, k, ogs.Add, ogs.NoTrans, stream, local=False)
 
     def Exchange(self, vs, k, stream=None):
-        self.ExchangeStart(vs, k, stream)
-        self.ExchangeFinish(vs, k, stream)
+        self._need_halo()
+        self._whole(vs, k, ogs.Add, ogs.NoTrans, stream, local=False)
         return vs
 
     def CombineStart(self, vs, k, stream=None):
         self._need_halo()
-        self._halo_start(vs, k, ogs.Add, ogs.Trans, stream)
+        self._start(vs, k, ogs.Add, ogs.Trans, stream)
 
     def CombineFinish(self, vs, k, stream=None):
-        self._halo_finish(vs, k, ogs.Add, ogs.Trans, stream)
+        self._finish(vs, k, ogs.Add, ogs.Trans, stream, local=False)
 
     def Combine(self, vs, k, stream=None):
-        self.CombineStart(vs, k, stream)
-        self.CombineFinish(vs, k, stream)
+        self._need_halo()
+        self._whole(vs, k, ogs.Add, ogs.Trans, stream, local=False)
         return vs
 
 
