@@ -247,11 +247,12 @@ ogs_status ogs_setup_ex(ogs_handle* out, int64_t N, int64_t* ids, int kind, int 
       (flags & OGS_SETUP_DEVICE_MAPS) ||
       (!host_only && !(flags & OGS_SETUP_HOST_MAPS) && N >= OGS_DEVICE_MAPS_MIN_N);
   try {
-    ogs_status s = device_maps ? build_device_maps(h, N, ids, kind, unique) : build_host_maps(h, N, ids, kind, unique);
-    if (s != OGS_OK) { delete h; return s; }
-    build_layout(h);
+    ogs_status s = device_maps ? build_device_maps(h, N, ids, kind, unique, true)
+                               : build_host_maps(h, N, ids, kind, unique);
+    if (s != OGS_OK) { release_device(h); delete h; return s; }
     h->host_only = host_only;
-    if (!h->host_only) {
+    if (!h->arena) build_layout(h);  // the device path built it already (unless the maps are empty)
+    if (!h->host_only && !h->arena) {
       s = upload_layout(h);
       if (s != OGS_OK) { release_device(h); delete h; return s; }
       cudaError_t e = cudaDeviceSynchronize();
@@ -526,8 +527,8 @@ ogs_status ogs_get_layout_stats(ogs_handle h, ogs_layout_stats* out) {
   if (!h || !out) return set_error(OGS_EINVAL, "ogs_get_layout_stats: NULL argument");
   std::memset(out, 0, sizeof(*out));
   for (int d = 1; d <= kDmax; ++d) out->rows_by_degree[d] = h->lay.n[d];
-  out->rows_by_degree[0] = static_cast<int64_t>(h->lay.g_rows.size());
-  out->nnz_general = static_cast<int64_t>(h->lay.g_colsT.size());
+  out->rows_by_degree[0] = h->lay.g_n;
+  out->nnz_general = h->lay.g_nnzT;
   out->ntiles = static_cast<int64_t>(h->lay.tiles.size());
   out->device_bytes = static_cast<int64_t>(h->arena_bytes);
   out->nphases = static_cast<int64_t>(h->lay.phases.size());

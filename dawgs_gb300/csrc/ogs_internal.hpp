@@ -184,6 +184,9 @@ struct HostLayout {
   std::vector<Tile> wtiles;  // exact-degree warp tiles, by first row
   std::vector<uint8_t> wemask;
   std::vector<Phase> phases;
+  int64_t g_n = 0, g_nnzT = 0;  // general-bucket rows and T entries
+  // lowest and highest local node each warp tile / general tile touches
+  std::vector<int64_t> wlo, whi, glo, ghi;
 };
 
 }  // namespace ogsgb
@@ -229,11 +232,15 @@ namespace ogsgb {
 // Host setup (ogs_setup.cpp).
 ogs_status build_host_maps(ogs_handle_s* h, int64_t N, int64_t* ids, int kind, int unique);
 // The same maps built on the current device (ogs_dsetup.cu).
-ogs_status build_device_maps(ogs_handle_s* h, int64_t N, int64_t* ids, int kind, int unique);
+ogs_status build_device_maps(ogs_handle_s* h, int64_t N, int64_t* ids, int kind, int unique, bool layout);
 void build_layout(ogs_handle_s* h);
 ogs_status upload_layout(ogs_handle_s* h);
 void release_device(ogs_handle_s* h);
-void build_phases(ogs_handle_s* h, int max_phases);
+void build_phases(ogs_handle_s* h, int max_phases);  // needs the tiles and their lo/hi
+// The maps' layout built on the current device from device CSR maps
+// (ogs_dsetup.cu): the arena, DevMaps and the host-side tile lists and phases.
+ogs_status build_device_layout(ogs_handle_s* h, const int32_t* d_rsT, const int32_t* d_ciT, const int32_t* d_rsN,
+                               const int32_t* d_ciN, void* stream);
 // DevMaps restricted to the tiles of one phase.
 DevMaps phase_maps(const DevMaps& m, const Phase& p);
 

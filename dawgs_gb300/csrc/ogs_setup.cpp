@@ -294,6 +294,31 @@ void build_layout(ogs_handle_s* h) {
   }
   L.tiles.insert(L.tiles.end(), L.gtiles.begin(), L.gtiles.end());
   std::stable_sort(L.tiles.begin(), L.tiles.end(), by_row);
+  L.g_n = static_cast<int64_t>(L.g_rows.size());
+  L.g_nnzT = static_cast<int64_t>(L.g_colsT.size());
+  // lowest and highest node of every tile (the host pipeline's slices)
+  L.wlo.assign(L.wtiles.size(), INT64_MAX);
+  L.whi.assign(L.wtiles.size(), -1);
+  for (size_t t = 0; t < L.wtiles.size(); ++t) {
+    const Tile& w = L.wtiles[t];
+    const int d = w.bucket;
+    const int64_t stride = static_cast<int64_t>(L.rows[d].size());
+    for (int q = 0; q < d; ++q)
+      for (int32_t r = 0; r < w.count; ++r) {
+        const int64_t c = L.cols[d][q * stride + w.begin + r];
+        L.wlo[t] = std::min(L.wlo[t], c);
+        L.whi[t] = std::max(L.whi[t], c);
+      }
+  }
+  L.glo.assign(L.gtiles.size(), INT64_MAX);
+  L.ghi.assign(L.gtiles.size(), -1);
+  for (size_t t = 0; t < L.gtiles.size(); ++t) {
+    const Tile& w = L.gtiles[t];
+    for (int32_t q = L.g_startsT[w.begin]; q < L.g_startsT[w.begin + w.count]; ++q) {
+      L.glo[t] = std::min<int64_t>(L.glo[t], L.g_colsT[q]);
+      L.ghi[t] = std::max<int64_t>(L.ghi[t], L.g_colsT[q]);
+    }
+  }
   build_phases(h, OGS_HOST_PHASES);
 }
 
@@ -333,22 +358,12 @@ void build_phases(ogs_handle_s* h, int max_phases) {
     ph.g1 = g;
     int64_t lo = INT64_MAX, hi = -1;
     for (int32_t t = ph.w0; t < ph.w1; ++t) {
-      const Tile& w = L.wtiles[t];
-      const int d = w.bucket;
-      const int64_t stride = static_cast<int64_t>(L.rows[d].size());
-      for (int q = 0; q < d; ++q)
-        for (int32_t r = 0; r < w.count; ++r) {
-          const int64_t c = L.cols[d][q * stride + w.begin + r];
-          lo = std::min(lo, c);
-          hi = std::max(hi, c);
-        }
+      lo = std::min(lo, L.wlo[t]);
+      hi = std::max(hi, L.whi[t]);
     }
     for (int32_t t = ph.g0; t < ph.g1; ++t) {
-      const Tile& w = L.gtiles[t];
-      for (int32_t q = L.g_startsT[w.begin]; q < L.g_startsT[w.begin + w.count]; ++q) {
-        lo = std::min<int64_t>(lo, L.g_colsT[q]);
-        hi = std::max<int64_t>(hi, L.g_colsT[q]);
-      }
+      lo = std::min(lo, L.glo[t]);
+      hi = std::max(hi, L.ghi[t]);
     }
     ph.lo = lo;
     ph.hi = hi;
