@@ -37,6 +37,10 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# e2e steps move the whole field both ways (113 MB at the default workload)
+# and refill the pinned buffer from the CPU: they are capped apart from the
+# kernel steps, which run long enough for several clock samples.
+E2E_STEPS = 30
 PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "ogs_async_kernel_gs_fp64_add_24x24x24_p7.md")
 FALLBACK_HBM_GBS = 6800.0
 TYPE_CODE = {"float32": 0, "float64": 1, "int32": 2, "int64": 3}
@@ -46,7 +50,7 @@ OP_CODE = {"add": 0, "mul": 1, "max": 2, "min": 3}
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--nx", type=int, default=24)
@@ -74,7 +78,9 @@ def parse():
 
 # ------------------------------------------------------------------ helpers
 class Clocks:
-    """nvidia-smi sampler running during the timed region."""
+    """nvidia-smi sampling the GPU every 50 ms while the timed region runs
+    (one streaming process, started before the region and stopped after it;
+    only the samples taken inside the region are kept)."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -82,30 +88,45 @@ class Clocks:
     def __init__(self, gpu_index: int):
         self.idx = gpu_index
         self.rows = []
-        self._stop = threading.Event()
+        self._all = []
+        self._proc = None
         self._t = None
+        self._t0 = self._t1 = None
 
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
-                                     timeout=5).stdout.strip()
-                if out:
-                    self.rows.append([x.strip() for x in out.split(",")])
-            except Exception:
-                return
-            self._stop.wait(0.2)
+    def _read(self):
+        for line in self._proc.stdout:
+            line = line.strip()
+            if line:
+                self._all.append((time.perf_counter(), [x.strip() for x in line.split(",")]))
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
-        self._t.start()
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                           "--format=csv,noheader,nounits", "-lms", "50"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+            deadline = time.perf_counter() + 5.0
+            while not self._all and time.perf_counter() < deadline:  # the sampler is running
+                time.sleep(0.01)
+        except OSError:
+            self._proc = None
+        self._t0 = time.perf_counter()
         return self
 
     def __exit__(self, *exc):
-        self._stop.set()
-        if self._t:
-            self._t.join(timeout=10)
+        self._t1 = time.perf_counter()
+        if self._proc is not None:
+            time.sleep(0.06)  # one more sample period
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+            if self._t:
+                self._t.join(timeout=5)
+        inside = [r for t, r in self._all if self._t0 <= t <= self._t1 + 0.06]
+        self.rows = inside if inside else [r for _, r in self._all[-1:]]
 
     def summary(self):
         if not self.rows:
@@ -543,18 +564,20 @@ def run_ours(a):
             host.copy_(torch.from_numpy(v))
             _lib.check(L.ogs_gather_scatter_host(h, host.data_ptr(), a.k, tcode, ocode, 0, stream.cuda_stream))
         et = []
-        for _ in range(a.steps):
+        e2e_steps = min(a.steps, E2E_STEPS)
+        for _ in range(e2e_steps):
             host.copy_(torch.from_numpy(v))
             flush_l2()
             barrier()
             t0 = time.perf_counter()
             _lib.check(L.ogs_gather_scatter_host(h, host.data_ptr(), a.k, tcode, ocode, 0, stream.cuda_stream))
             et.append(time.perf_counter() - t0)
-        t_e2e, _, e2e_value = aggregate_over_ranks(sum(et), g.NgatherGlobal * a.steps, dev)
+        t_e2e, _, e2e_value = aggregate_over_ranks(sum(et), g.NgatherGlobal * e2e_steps, dev)
         nbytes = a.k * ids.size * s
         e2e = {"value": e2e_value, "unit": "DOFS/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-               "ms_per_step": 1e3 * t_e2e / a.steps, "api": "ogs_gather_scatter_host (C ABI)"}
+               "ms_per_step": 1e3 * t_e2e / e2e_steps, "steps": e2e_steps,
+               "api": "ogs_gather_scatter_host (C ABI)"}
 
     # correctness of the timed configuration on this run's own output
     work.copy_(pristine)
