@@ -210,10 +210,10 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
 
 template <typename T, int OP, int MODE, int KL, bool PLAIN>
 inline int async_grid(int64_t nitems) {
-  static int cached_dev = -1, cached = 0;
+  static DeviceCache cache;
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev != cached_dev) {
+  const int cached = cache.get(dev, [dev] {
     int bps = 0, sms = 0;
     // above 48 KB (more entries per lane) the dynamic shared memory must be opted into
     if (async_smem_bytes<T>() > 48 * 1024)
@@ -222,9 +222,8 @@ inline int async_grid(int64_t nitems) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_async_kernel<T, OP, MODE, KL, PLAIN>, kBlock,
                                                   async_smem_bytes<T>());
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cached = (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1);
-    cached_dev = dev;
-  }
+    return (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1);
+  });
   const int64_t need = (nitems + (kBlock / 32) - 1) / (kBlock / 32);
   return static_cast<int>(need < cached ? need : cached);
 }

@@ -147,19 +147,19 @@ __global__ void __launch_bounds__(kBlock, OGS_BATCH_MINB) ogs_batch_kernel(const
 
 template <typename T>
 inline int batch_blocks_per_sm(int* sms) {
-  static int cached_dev = -1, cached_bps = 0, cached_sms = 0;
+  static DeviceCache bps_cache, sms_cache;
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev != cached_dev) {
-    int bps = 0, s = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_batch_kernel<T>, kBlock, 0);
+  *sms = sms_cache.get(dev, [dev] {
+    int s = 0;
     cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
-    cached_bps = bps > 0 ? bps : 1;
-    cached_sms = s > 0 ? s : 1;
-    cached_dev = dev;
-  }
-  *sms = cached_sms;
-  return cached_bps;
+    return s > 0 ? s : 1;
+  });
+  return bps_cache.get(dev, [] {
+    int bps = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_batch_kernel<T>, kBlock, 0);
+    return bps > 0 ? bps : 1;
+  });
 }
 
 // grid <= 0: resident CTAs on every SM.

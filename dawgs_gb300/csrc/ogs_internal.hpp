@@ -4,6 +4,7 @@
 // (ogs_kern_*.cu).
 #pragma once
 
+#include <atomic>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -17,6 +18,24 @@
 #endif
 
 namespace ogsgb {
+
+// A launch figure per device (CTAs per SM, SM count), computed on first use.
+// Concurrent first uses compute the same value, so filling it without a lock
+// is safe; the atomics keep the sharing well defined.
+struct DeviceCache {
+  static constexpr int kDevices = 64;
+  std::atomic<int> v[kDevices];
+  template <typename F>
+  int get(int dev, F compute) {
+    if (dev < 0 || dev >= kDevices) return compute();
+    int x = v[dev].load(std::memory_order_acquire);
+    if (x == 0) {
+      x = compute();
+      v[dev].store(x, std::memory_order_release);
+    }
+    return x;
+  }
+};
 
 // Rows of exact degree 1..kDmax are stored in fixed-width buckets; rows of a
 // larger degree go to one general CSR bucket.

@@ -229,16 +229,15 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const D
 // CTAs of the warp kernel resident per SM, once per instantiation and device.
 template <typename T, int OP, int MODE, int KL>
 inline int warp_grid(int64_t nitems) {
-  static int cached_dev = -1, cached = 0;
+  static DeviceCache cache;
   int dev = 0;
   cudaGetDevice(&dev);
-  if (dev != cached_dev) {
+  const int cached = cache.get(dev, [dev] {
     int bps = 0, sms = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_warp_kernel<T, OP, MODE, KL>, kBlock, 0);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cached = (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1);
-    cached_dev = dev;
-  }
+    return (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1);
+  });
   const int64_t need = (nitems + (kBlock / 32) - 1) / (kBlock / 32);
   return static_cast<int>(need < cached ? need : cached);
 }
