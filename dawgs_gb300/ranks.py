@@ -409,5 +409,58 @@ class ranks_ogs_t:
         self._whole(vs, k, ogs.Add, ogs.Trans, stream, local=False)
         return vs
 
+    # -- halo_t made from a gather (halo_t::SetupFromGather, ogsSetup.cpp:888-
+    # 913; the gathered_halo branches of ogsHalo.cpp:39-359): the vectors are
+    # gathered ones, [local rows | halo rows, those with a positive member
+    # first], and the halo rows are copied instead of gathered --
+    def gathered_sizes(self):
+        """(NlocalT + NhaloT) rows of each rank's gathered vector."""
+        return [m["nlocal"] + m["nhalo"] for m in self.maps]
+
+    def _gathered(self, gvs, k, trans, stream):
+        import torch
+        if self.kind == HALO:
+            raise ValueError("a gathered halo comes from an Unsigned or Signed setup")
+        which = self._which(trans)
+        off, send_ids, recv_src = self.plan[which]
+        send, bufs = self._buffers(gvs[0].dtype, k)
+        main = self._fork(stream)
+        sent = []
+        for r, (m, s) in enumerate(zip(self.maps, self._streams())):
+            nl, nh, nhp = m["nlocal"], m["nhalo"], m["nhaloP"]
+            rows = nhp if which == "N" else nh  # NoTrans sends the owned rows, Trans all halo rows
+            with torch.cuda.stream(s):
+                if rows:
+                    bufs[r][: rows * k].copy_(gvs[r][nl * k:(nl + rows) * k])
+            ns = send_ids[r].numel()
+            if ns:
+                ogs.extract(send[off[r] * k:(off[r] + ns) * k], bufs[r], send_ids[r], k, stream=s)
+            ev = torch.cuda.Event()
+            ev.record(s)
+            sent.append(ev)
+        for j, (m, s) in enumerate(zip(self.maps, self._streams())):
+            self._recv(j, k, which, sent, s, gvs[0].dtype)
+            nl, nh, nhp = m["nlocal"], m["nhalo"], m["nhaloP"]
+            if not nh:
+                continue
+            post, cols = (self.postN[j], m["postN_cols"]) if which == "N" else (self.postT[j], m["postT_cols"])
+            post.Gather(bufs[j][: nh * k], bufs[j][: cols * k], k, ogs.Add, ogs.Trans, stream=s)
+            with torch.cuda.stream(s):
+                if which == "N":  # the owners' values into the rows this rank does not own
+                    if nh > nhp:
+                        gvs[j][(nl + nhp) * k:(nl + nh) * k].copy_(bufs[j][nhp * k:nh * k])
+                elif nhp:  # the combined values into the owned rows
+                    gvs[j][nl * k:(nl + nhp) * k].copy_(bufs[j][: nhp * k])
+        self._join(main)
+        return gvs
+
+    def GatheredExchange(self, gvs, k, stream=None):
+        """Every copy of a halo row gets its owner's value (Add, NoTrans)."""
+        return self._gathered(gvs, k, ogs.NoTrans, stream)
+
+    def GatheredCombine(self, gvs, k, stream=None):
+        """The owner's copy of a halo row gets the sum over all copies (Add, Trans)."""
+        return self._gathered(gvs, k, ogs.Trans, stream)
+
 
 __all__ = ["build_rank_maps", "ranks_ogs_t", "UNSIGNED", "SIGNED", "HALO"]

@@ -162,3 +162,69 @@ def signed_parts(parts, seed, kind):
                 q[n] = b
         out.append(q)
     return out
+
+
+def gathered_rows(ids_list, kind):
+    """Each rank's gathered-vector rows by id: (local ids in row order, halo
+    ids in row order, number of halo rows with a positive member).  Rows by
+    first appearance on the rank, in four classes numbered apart: local rows
+    with a positive member, the other local rows, halo rows with a positive
+    member, the other halo rows (ogsSetup.cpp:406-433)."""
+    idsl = [np.asarray(x, dtype=np.int64) for x in ids_list]
+    absids = [np.abs(x) for x in idsl]
+    holders = {}
+    for r, a in enumerate(absids):
+        for b in np.unique(a[a != 0]):
+            holders.setdefault(int(b), []).append(r)
+    out = []
+    for x, a in zip(idsl, absids):
+        order = _rows_by_first_appearance(a)
+        pos = set(int(b) for b in np.unique(a[x > 0])) if kind == "signed" else set(int(b) for b in order)
+        loc = [int(b) for b in order if len(holders[int(b)]) == 1]
+        hal = [int(b) for b in order if len(holders[int(b)]) > 1]
+        loc = [b for b in loc if b in pos] + [b for b in loc if b not in pos]
+        halp = [b for b in hal if b in pos]
+        out.append((loc, halp + [b for b in hal if b not in pos], len(halp)))
+    return out, holders
+
+
+def gathered_exchange(ids_list, gvs, k, kind, trans):
+    """Expected gathered vectors after a halo_t made from a gather runs
+    Exchange (trans "notrans": each copy of a halo row not owned on its rank
+    gets identity + the owners' values, ogsHalo.cpp:55-146) or Combine (trans
+    "trans": each owned copy gets identity + its own value + the other copies'
+    values by ascending rank, ogsHalo.cpp:203-290).  gvs: per rank
+    [local rows | halo rows] * k."""
+    rows, holders = gathered_rows(ids_list, kind)
+    dtype = gvs[0].dtype
+    where = []  # per rank: halo id -> (row in the gathered vector, owned)
+    for loc, hal, nhp in rows:
+        where.append({b: (len(loc) + h, h < nhp) for h, b in enumerate(hal)})
+    out = [g.copy() for g in gvs]
+    ident = np.full(k, _identity(dtype, "add"), dtype)
+    for j, (loc, hal, nhp) in enumerate(rows):
+        todo = [b for b in hal if (not where[j][b][1]) == (trans == "notrans")]
+        cid, vals, empty = [], [], set()
+        for b in todo:
+            if trans == "notrans":
+                seq = [s for s in holders[b] if s != j and where[s][b][1]]
+            else:
+                seq = [j] + [s for s in holders[b] if s != j]
+            if not seq:
+                empty.add(b)
+            for s in seq:
+                row = where[s][b][0]
+                cid.append(b)
+                vals.append(gvs[s][row * k:(row + 1) * k])
+        val = {b: ident for b in empty}
+        if cid:
+            order = [b for b in todo if b not in empty]
+            gv = np.zeros(len(order) * k, dtype)
+            OracleOgs(np.asarray(cid, np.int64), "unsigned").gather(gv, np.concatenate(vals).astype(dtype), k,
+                                                                    "add", "trans")
+            for i, b in enumerate(order):
+                val[b] = gv[i * k:(i + 1) * k]
+        for b in todo:
+            row = where[j][b][0]
+            out[j][row * k:(row + 1) * k] = val[b]
+    return out

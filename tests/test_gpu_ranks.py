@@ -143,3 +143,26 @@ def test_operator_empty_rows_gather_identity(cuda, op, ident):
     torch.cuda.synchronize()
     assert v.cpu().tolist() == [first, 2.0, first, 4.0]
 
+
+@pytest.mark.parametrize("key", PARTS[:4], ids=lambda p: f"{p[0]}-{p[1]}-{p[2]}")
+@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int64], ids=lambda t: np.dtype(t).name)
+@pytest.mark.parametrize("kind", ["signed", "unsigned"])
+@pytest.mark.parametrize("trans", ["notrans", "trans"])
+def test_gathered_halo_matches_oracle(cuda, oracle_mod, key, dtype, kind, trans):
+    """halo_t made from a gather: Exchange (NoTrans) and Combine (Trans) on
+    gathered vectors [local rows | halo rows]."""
+    box, R, how = key
+    parts = oranks.partition_box(*box, R, how=how, seed=17)
+    if kind == "signed":
+        parts = oranks.signed_parts(parts, 5, "halo")
+    rk = ranks.ranks_ogs_t(parts, ranks.SIGNED if kind == "signed" else ranks.UNSIGNED)
+    for k in (1, 3):
+        gvs = [values(n * k, dtype, "add", seed=90 + i + k) for i, n in enumerate(rk.gathered_sizes())]
+        want = oranks.gathered_exchange(parts, gvs, k, kind, trans)
+        ds = [torch.from_numpy(g.copy()).cuda() for g in gvs]
+        (rk.GatheredExchange if trans == "notrans" else rk.GatheredCombine)(ds, k)
+        torch.cuda.synchronize()
+        for r, (d, w) in enumerate(zip(ds, want)):
+            got = d.cpu().numpy()
+            assert same_bits(got, w), (key, kind, trans, k, r, first_diff(got, w))
+
