@@ -217,6 +217,7 @@ class ranks_ogs_t:
         import torch
         self.R = len(ids_list)
         self.kind = int(kind)
+        self._ids = [np.asarray(x, dtype=np.int64) for x in ids_list]
         self.maps = build_rank_maps(ids_list, self.kind)
         self.local, self.halo, self.postT, self.postN = [], [], [], []
         for m in self.maps:
@@ -407,6 +408,94 @@ class ranks_ogs_t:
     def Combine(self, vs, k, stream=None):
         self._need_halo()
         self._whole(vs, k, ogs.Add, ogs.Trans, stream, local=False)
+        return vs
+
+    # -- ogs_t Gather and Scatter (ogs.cpp:202-298, 392-488): gathered
+    # vectors are [local rows | halo rows]; only Trans Gather and NoTrans
+    # Scatter exchange --
+    def gather_defined(self):
+        """Every id has exactly one positive copy over all ranks (ogsSetup.cpp:276-282)."""
+        if not hasattr(self, "_gdef"):
+            ids = np.concatenate([np.asarray(x, np.int64) for x in self._ids]) if self.R else np.zeros(0, np.int64)
+            a = np.abs(ids[ids != 0])
+            allu = _distinct(a)
+            pos = np.sort(ids[ids > 0])
+            cnt = np.searchsorted(pos, allu, side="right") - np.searchsorted(pos, allu, side="left")
+            self._gdef = bool(self.kind == SIGNED and np.all(cnt == 1))
+        return self._gdef
+
+    def gather_sizes(self, trans=ogs.Trans):
+        """Rows of each rank's gathered vector: NlocalT + NhaloP (NhaloT for Sym)."""
+        sym = int(trans) == int(ogs.Sym)
+        return [m["nlocal"] + (m["nhalo"] if sym else m["nhaloP"]) for m in self.maps]
+
+    def _need_gather(self):
+        if not self.gather_defined():
+            raise ValueError("Gather operation not well-defined.")  # ogsSetup.cpp:861-864
+
+    def Gather(self, gvs, vs, k, op=ogs.Add, trans=ogs.Trans, stream=None):
+        import torch
+        self._need_gather()
+        t = int(trans)
+        main = self._fork(stream)
+        if t == int(ogs.Trans):
+            sent = self._sends(vs, k, op, trans, "T")
+        for r, (m, s) in enumerate(zip(self.maps, self._streams())):
+            nl = m["nlocal"]
+            if nl:
+                self.local[r].Gather(gvs[r][: nl * k], vs[r], k, op, trans, stream=s)
+            if t != int(ogs.Trans) and m["nhalo"]:
+                rows = m["nhalo"] if t == int(ogs.Sym) else m["nhaloP"]
+                if rows:
+                    self.halo[r].Gather(gvs[r][nl * k:(nl + rows) * k], vs[r], k, op, trans, stream=s)
+        if t == int(ogs.Trans):
+            _, bufs = self._buffers(vs[0].dtype, k)
+            for j, (m, s) in enumerate(zip(self.maps, self._streams())):
+                self._recv(j, k, "T", sent, s, vs[0].dtype)
+                nl, nh, nhp = m["nlocal"], m["nhalo"], m["nhaloP"]
+                if not nh:
+                    continue
+                self.postT[j].Gather(bufs[j][: nh * k], bufs[j][: m["postT_cols"] * k], k, op, ogs.Trans,
+                                     stream=s)
+                if nhp:
+                    with torch.cuda.stream(s):
+                        gvs[j][nl * k:(nl + nhp) * k].copy_(bufs[j][: nhp * k])
+        self._join(main)
+        return gvs
+
+    def Scatter(self, vs, gvs, k, trans=ogs.NoTrans, stream=None):
+        import torch
+        self._need_gather()
+        t = int(trans)
+        main = self._fork(stream)
+        if t == int(ogs.NoTrans):
+            off, send_ids, _ = self.plan["N"]
+            send, bufs = self._buffers(vs[0].dtype, k)
+            sent = []
+            for r, (m, s) in enumerate(zip(self.maps, self._streams())):
+                nl, nhp = m["nlocal"], m["nhaloP"]
+                with torch.cuda.stream(s):
+                    if nhp:
+                        bufs[r][: nhp * k].copy_(gvs[r][nl * k:(nl + nhp) * k])
+                ns = send_ids[r].numel()
+                if ns:
+                    ogs.extract(send[off[r] * k:(off[r] + ns) * k], bufs[r], send_ids[r], k, stream=s)
+                ev = torch.cuda.Event()
+                ev.record(s)
+                sent.append(ev)
+        for r, (m, s) in enumerate(zip(self.maps, self._streams())):
+            nl = m["nlocal"]
+            if nl:
+                self.local[r].Scatter(vs[r], gvs[r][: nl * k], k, trans, stream=s)
+            # Trans reads halo rows [0, NhaloP), Sym [0, NhaloT), after the local rows
+            rows = m["nhalo"] if t == int(ogs.Sym) else m["nhaloP"]
+            if t != int(ogs.NoTrans) and rows:
+                self.halo[r].Scatter(vs[r], gvs[r][nl * k:(nl + rows) * k], k, trans, stream=s)
+        if t == int(ogs.NoTrans):
+            for j, (m, s) in enumerate(zip(self.maps, self._streams())):
+                self._recv(j, k, "N", sent, s, vs[0].dtype)
+                self._post_scatter(j, vs, k, ogs.Add, ogs.NoTrans, "N", s)
+        self._join(main)
         return vs
 
     # -- halo_t made from a gather (halo_t::SetupFromGather, ogsSetup.cpp:888-

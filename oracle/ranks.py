@@ -228,3 +228,103 @@ def gathered_exchange(ids_list, gvs, k, kind, trans):
             row = where[j][b][0]
             out[j][row * k:(row + 1) * k] = val[b]
     return out
+
+
+def _fold_lists(lists, k, op, dtype):
+    """fold from the op identity over each list of k-vectors, in list order
+    (through OracleOgs: entries of row i carry id i + 1, rows in order)."""
+    out = [None] * len(lists)
+    cid, vals = [], []
+    for i, lst in enumerate(lists):
+        if not lst:
+            out[i] = np.full(k, _identity(dtype, op), dtype)
+        for x in lst:
+            cid.append(i + 1)
+            vals.append(x)
+    if cid:
+        present = [i for i, lst in enumerate(lists) if lst]
+        gv = np.zeros(len(present) * k, dtype)
+        OracleOgs(np.asarray(cid, np.int64), "unsigned").gather(gv, np.concatenate(vals).astype(dtype), k, op,
+                                                                "trans")
+        for n, i in enumerate(present):
+            out[i] = gv[n * k:(n + 1) * k]
+    return out
+
+
+def _members(ids_list):
+    """Per rank: |id| -> (all members, positive members), ascending local index."""
+    out = []
+    for x in ids_list:
+        x = np.asarray(x, np.int64)
+        m = {}
+        for n in np.nonzero(x)[0]:
+            b = int(abs(x[n]))
+            t, p = m.setdefault(b, ([], []))
+            t.append(int(n))
+            if x[n] > 0:
+                p.append(int(n))
+        out.append(m)
+    return out
+
+
+def ranks_gather(ids_list, vs, k, op, trans):
+    """Expected gathered vectors of a multi-rank Signed ogs_t Gather
+    (ogs.cpp:202-298): [local rows | halo rows with a positive member (all
+    halo rows for Sym)]; local rows and NoTrans/Sym halo rows fold this
+    rank's members (N members for NoTrans), Trans halo rows fold this rank's
+    partial and then the other holders' partials by ascending rank."""
+    rows, holders = gathered_rows(ids_list, "signed")
+    mem = _members(ids_list)
+    dtype = vs[0].dtype
+    sel = (lambda b, r: mem[r][b][1]) if trans == "notrans" else (lambda b, r: mem[r][b][0])
+    out = []
+    for r, (loc, hal, nhp) in enumerate(rows):
+        v = vs[r]
+        val = lambda n: v[n * k:(n + 1) * k]
+        lists = [[val(n) for n in sel(b, r)] for b in loc]
+        hrows = hal if trans == "sym" else hal[:nhp]
+        if trans == "trans":
+            for b in hrows:
+                seq = [r] + [s for s in holders[b] if s != r]
+                lists.append([_fold_lists([[vs[s][n * k:(n + 1) * k] for n in mem[s][b][0]]], k, op, dtype)[0]
+                              for s in seq])
+        else:
+            lists += [[val(n) for n in sel(b, r)] for b in hrows]
+        folded = _fold_lists(lists, k, op, dtype)
+        out.append(np.concatenate(folded) if folded else np.zeros(0, dtype))
+    return out
+
+
+def ranks_scatter(ids_list, vs, gvs, k, trans):
+    """Expected local vectors after a multi-rank Signed ogs_t Scatter
+    (ogs.cpp:392-488) of gathered vectors [local rows | halo rows]: Trans
+    writes each row's value to its positive members, NoTrans and Sym to all
+    members; NoTrans halo rows take, from the op identity (Add), the value of
+    the rank holding the positive copy (exchanged)."""
+    rows, holders = gathered_rows(ids_list, "signed")
+    mem = _members(ids_list)
+    dtype = vs[0].dtype
+    where = [{b: (len(loc) + h) for h, b in enumerate(hal)} for loc, hal, _ in rows]
+    owner = {b: r for r, (loc, hal, nhp) in enumerate(rows) for b in hal[:nhp]}
+    out = [v.copy() for v in vs]
+    for r, (loc, hal, nhp) in enumerate(rows):
+        g = gvs[r]
+        tgt = (lambda b: mem[r][b][1]) if trans == "trans" else (lambda b: mem[r][b][0])
+        for i, b in enumerate(loc):
+            for n in tgt(b):
+                out[r][n * k:(n + 1) * k] = g[i * k:(i + 1) * k]
+        if trans == "notrans":
+            lists = []
+            for b in hal:
+                o = owner.get(b)
+                lists.append([] if o is None else [gvs[o][where[o][b] * k:(where[o][b] + 1) * k]])
+            vals = _fold_lists(lists, k, "add", dtype)
+            for b, x in zip(hal, vals):
+                for n in mem[r][b][0]:
+                    out[r][n * k:(n + 1) * k] = x
+        else:
+            for h, b in enumerate(hal if trans == "sym" else hal[:nhp]):
+                row = len(loc) + h
+                for n in tgt(b):
+                    out[r][n * k:(n + 1) * k] = g[row * k:(row + 1) * k]
+    return out

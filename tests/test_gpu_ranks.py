@@ -166,3 +166,44 @@ def test_gathered_halo_matches_oracle(cuda, oracle_mod, key, dtype, kind, trans)
             got = d.cpu().numpy()
             assert same_bits(got, w), (key, kind, trans, k, r, first_diff(got, w))
 
+
+@pytest.mark.parametrize("key", PARTS[:4], ids=lambda p: f"{p[0]}-{p[1]}-{p[2]}")
+@pytest.mark.parametrize("dtype", [np.float64, np.float32, np.int32], ids=lambda t: np.dtype(t).name)
+@pytest.mark.parametrize("trans", ["trans", "notrans", "sym"])
+def test_ranks_gather_and_scatter_match_oracle(cuda, oracle_mod, key, dtype, trans):
+    """Multi-rank ogs_t Gather (Trans exchanges) and Scatter (NoTrans
+    exchanges) on a Signed setup with one positive copy per id."""
+    box, R, how = key
+    parts = oranks.signed_parts(oranks.partition_box(*box, R, how=how, seed=17), 5, "halo")
+    rk = ranks.ranks_ogs_t(parts, ranks.SIGNED)
+    assert rk.gather_defined()
+    T = {"trans": ogs.Trans, "notrans": ogs.NoTrans, "sym": ogs.Sym}[trans]
+    for k in (1, 2):
+        for op in ("add", "max"):
+            vs = [values(p.size * k, dtype, op, seed=110 + i + k) for i, p in enumerate(parts)]
+            want = oranks.ranks_gather(parts, vs, k, op, trans)
+            gds = [torch.zeros(n * k, dtype=torch.from_numpy(vs[0]).dtype, device="cuda")
+                   for n in rk.gather_sizes(T)]
+            rk.Gather(gds, [torch.from_numpy(v).cuda() for v in vs], k, ogs.Op[op.capitalize()], T)
+            torch.cuda.synchronize()
+            for r, (d, w) in enumerate(zip(gds, want)):
+                got = d.cpu().numpy()
+                assert same_bits(got, w), ("gather", key, trans, op, k, r, first_diff(got, w))
+        gvs = [values(n * k, dtype, "add", seed=130 + i + k) for i, n in enumerate(rk.gather_sizes(T))]
+        v0 = [values(p.size * k, dtype, "add", seed=150 + i) for i, p in enumerate(parts)]
+        want = oranks.ranks_scatter(parts, v0, gvs, k, trans)
+        ds = [torch.from_numpy(v.copy()).cuda() for v in v0]
+        rk.Scatter(ds, [torch.from_numpy(g).cuda() for g in gvs], k, T)
+        torch.cuda.synchronize()
+        for r, (d, w) in enumerate(zip(ds, want)):
+            got = d.cpu().numpy()
+            assert same_bits(got, w), ("scatter", key, trans, k, r, first_diff(got, w))
+
+
+def test_ranks_gather_refused_when_not_defined(cuda):
+    parts = oranks.partition_box(4, 4, 3, 2, 2, how="slabs")  # Unsigned: every copy positive
+    rk = ranks.ranks_ogs_t(parts, ranks.UNSIGNED)
+    assert not rk.gather_defined()
+    with pytest.raises(ValueError):
+        rk.Gather([torch.zeros(1, device="cuda")] * 2, [torch.zeros(p.size, device="cuda") for p in parts], 1)
+
