@@ -263,6 +263,7 @@ ogs_status ogs_setup_ex(ogs_handle* out, int64_t N, int64_t* ids, int kind, int 
       }
     }
   } catch (const std::bad_alloc&) {
+    release_device(h);  // the device setup may have made the arena already
     delete h;
     return set_error(OGS_ENOMEM, "ogs_setup: out of host memory");
   }

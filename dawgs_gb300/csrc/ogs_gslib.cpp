@@ -108,6 +108,7 @@ ogs_status ogs_gslib_setup(ogs_handle* out, const int64_t* ids, int64_t n, unsig
       if (s != OGS_OK) { release_device(h); delete h; return s; }
     }
   } catch (const std::bad_alloc&) {
+    release_device(h);
     delete h;
     return set_error(OGS_ENOMEM, "ogs_gslib_setup: out of host memory");
   }

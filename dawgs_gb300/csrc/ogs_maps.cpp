@@ -119,6 +119,7 @@ extern "C" ogs_status ogs_setup_maps(ogs_handle* out, int64_t N, int64_t NrowsN,
       }
     }
   } catch (const std::bad_alloc&) {
+    release_device(h);
     delete h;
     return set_error(OGS_ENOMEM, "ogs_setup_maps: out of host memory");
   }
