@@ -11,15 +11,18 @@
 // registers while in flight, so each warp keeps two items' values and a
 // third item's column ids in flight:
 //
-//   iteration for item i:  issue gathers of item i+W into stage (s+1) % 3
+//   iteration for item i:  issue gathers of item i+W into stage (s+1) % 2
 //                          issue column-id loads of item i+2W (registers)
 //                          wait for the gathers of item i (stage s)
 //                          fold item i from shared memory, store
 //
 // Every lane gathers and later folds its own entries only, so no barrier of
 // any kind is needed: cp.async.wait_group makes a thread's own completed
-// copies visible to it.  With three stages, the stage an iteration refills
-// was read two iterations earlier.
+// copies visible to it.  Two stages suffice: the stage an iteration refills
+// is the one the previous iteration read, and every value read there was
+// consumed by the fold (in-order issue, and the asm's memory clobber keeps
+// the compiler from moving the reads) before this iteration's cp.async
+// issues.  A third stage only takes shared memory from L1 (measured slower).
 #pragma once
 
 #include <cstdint>
@@ -32,7 +35,10 @@
 
 namespace ogsgb {
 
-constexpr int kAsyncStages = 3;
+#ifndef OGS_ASYNC_STAGES
+#define OGS_ASYNC_STAGES 2
+#endif
+constexpr int kAsyncStages = OGS_ASYNC_STAGES;
 
 template <typename T>
 __device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem) {
