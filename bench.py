@@ -623,7 +623,7 @@ def run_ours(a):
                    "global_dofs": int(g.NgatherGlobal), "k": a.k,
                    "l2": f"flushed between steps ({flush.numel() * 4 >> 20} MiB write then read)",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "tiles": stats["ntiles"]},
+                   "warp_tiles": stats["nwarp_tiles"], "general_tiles": stats["ngeneral_tiles"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profiled_traffic(),
                      "warm": {"ms_per_step": warm_per_step * 1e3, "achieved": nbytes_alg / warm_per_step / 1e9,

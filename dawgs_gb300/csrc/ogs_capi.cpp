@@ -531,6 +531,8 @@ ogs_status ogs_get_layout_stats(ogs_handle h, ogs_layout_stats* out) {
   out->rows_by_degree[0] = h->lay.g_n;
   out->nnz_general = h->lay.g_nnzT;
   out->ntiles = static_cast<int64_t>(h->lay.tiles.size());
+  out->nwarp_tiles = static_cast<int64_t>(h->lay.wtiles.size());
+  out->ngeneral_tiles = static_cast<int64_t>(h->lay.gtiles.size());
   out->device_bytes = static_cast<int64_t>(h->arena_bytes);
   out->nphases = static_cast<int64_t>(h->lay.phases.size());
   for (size_t p = 0; p < h->lay.phases.size() && p < 32; ++p) {

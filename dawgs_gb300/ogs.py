@@ -267,7 +267,8 @@ class ogs_t:
         check(lib().ogs_get_layout_stats(self.handle, C.byref(s)))
         return {"rows_by_degree": {d: int(s.rows_by_degree[d]) for d in range(1, 9) if s.rows_by_degree[d]},
                 "rows_general": int(s.rows_by_degree[0]), "nnz_general": int(s.nnz_general),
-                "ntiles": int(s.ntiles), "device_bytes": int(s.device_bytes),
+                "ntiles": int(s.ntiles), "nwarp_tiles": int(s.nwarp_tiles),
+                "ngeneral_tiles": int(s.ngeneral_tiles), "device_bytes": int(s.device_bytes),
                 "phases": [tuple(int(x) for x in s.phases[p]) for p in range(int(s.nphases))]}
 
 

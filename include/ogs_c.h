@@ -77,11 +77,14 @@ typedef struct {
 typedef struct {
   int64_t rows_by_degree[9]; /* [d] rows of exact degree d (1..8); [0] rows above 8 */
   int64_t nnz_general;       /* entries in rows above degree 8 */
-  int64_t ntiles;            /* work tiles in one launch over the whole map */
+  int64_t ntiles;            /* 256-thread block tiles of the whole map (one-CTA-per-tile kernels) */
   int64_t device_bytes;      /* device memory held by the handle's maps */
   int64_t nphases;           /* slices of the host-buffer pipeline (at most 32) */
   int64_t phases[32][4];     /* per slice: lowest and highest node it touches, end of its
                                 host->device chunk, end of the nodes final after it */
+  int64_t nwarp_tiles;       /* warp tiles (32 lanes x 8 entries, exact degree): the work
+                                items of the GatherScatter/Gather/Scatter launches */
+  int64_t ngeneral_tiles;    /* tiles of rows above degree 8 */
 } ogs_layout_stats;
 
 /* ogs_t::Setup (include/ogs.hpp:221-228; libs/ogs/ogsSetup.cpp:69-190).

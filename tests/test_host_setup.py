@@ -71,6 +71,10 @@ def test_c2_box_counts_match_closed_form(oracle_mod):
     assert g.NgatherGlobal == cf["global"] == 4826809
     st = g.layout_stats()
     assert st["rows_by_degree"] == cf["rows_by_degree"] == {1: 3112136, 2: 1470804, 4: 231702, 8: 12167}
+    # warp tiles: 32 lanes x 8 entries, i.e. 32 * (8 // d) rows of degree d, per bucket
+    want = sum(-(-n // (32 * max(1, 8 // d))) for d, n in cf["rows_by_degree"].items())
+    assert st["nwarp_tiles"] == want == 27650
+    assert st["ngeneral_tiles"] == 0
 
 
 @pytest.mark.parametrize("name", ["c1_box", "box_permuted", "random_multiplicity", "high_degree"])
