@@ -35,40 +35,18 @@
 
 namespace ogsgb {
 
-// Full tiles (all but the last of each bucket) take a copy of the per-item
-// code without the per-row bounds checks, chosen by a warp-uniform branch.
-#ifndef OGS_ASYNC_FULL
-#define OGS_ASYNC_FULL 0
-#endif
-
 #ifndef OGS_ASYNC_STAGES
 #define OGS_ASYNC_STAGES 2
 #endif
 constexpr int kAsyncStages = OGS_ASYNC_STAGES;
 
-// L2 prefetch size attached to each gather (0: none, else 64, 128 or 256
-// bytes): a miss then brings the neighbouring sectors of the line into L2,
-// where the gathers of nearby rows find them.
-#ifndef OGS_ASYNC_PREFETCH
-#define OGS_ASYNC_PREFETCH 0
-#endif
-#if OGS_ASYNC_PREFETCH == 64
-#define OGS_CPA_HINT ".L2::64B"
-#elif OGS_ASYNC_PREFETCH == 128
-#define OGS_CPA_HINT ".L2::128B"
-#elif OGS_ASYNC_PREFETCH == 256
-#define OGS_CPA_HINT ".L2::256B"
-#else
-#define OGS_CPA_HINT ""
-#endif
-
 template <typename T>
 __device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem) {
   const unsigned s = static_cast<unsigned>(__cvta_generic_to_shared(smem));
   if (sizeof(T) == 8)
-    asm volatile("cp.async.ca.shared.global" OGS_CPA_HINT " [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
   else
-    asm volatile("cp.async.ca.shared.global" OGS_CPA_HINT " [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
 }
 
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
@@ -79,13 +57,13 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 // Entry e of this lane lives at stage[e * 32 + lane].
-template <typename T, int MODE, int D, bool FULL = false>
+template <typename T, int MODE, int D>
 __device__ __forceinline__ void async_issue_vals(const WarpState& s, const T* src, const T* gv, int64_t stride, int K,
                                                  int k, bool gmask, int lane, T* stage) {
   constexpr int RPT = warp_rows_per_lane(D);
 #pragma unroll
   for (int j = 0; j < RPT; ++j) {
-    if (FULL || j * 32 + lane < s.cnt) {
+    if (j * 32 + lane < s.cnt) {
       if (MODE == kModeScatter) {
         cp_async_elem(stage + j * 32 + lane, gv + static_cast<int64_t>(s.R[j]) * K + k);
       } else {
@@ -98,13 +76,13 @@ __device__ __forceinline__ void async_issue_vals(const WarpState& s, const T* sr
   }
 }
 
-template <typename T, int MODE, int D, bool FULL = false>
+template <typename T, int MODE, int D>
 __device__ __forceinline__ void async_read_vals(const WarpState& s, bool gmask, int lane, const T* stage,
                                                 T (&V)[kWarpSlots]) {
   constexpr int RPT = warp_rows_per_lane(D);
 #pragma unroll
   for (int j = 0; j < RPT; ++j) {
-    if (FULL || j * 32 + lane < s.cnt) {
+    if (j * 32 + lane < s.cnt) {
       if (MODE == kModeScatter) {
         V[j] = stage[j * 32 + lane];
       } else {
@@ -165,14 +143,7 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
     if (i + 2 * W < nitems) nn = m.wtiles[tile_of(i + 2 * W)];
   }
   WarpState scur, snxt;
-#define OGS_A_FULL(D, CNT) (OGS_ASYNC_FULL && PLAIN && (CNT) == warp_rows_per_tile(D))
-#define OGS_A_LOAD(D, TILE, TI, S)                                                        \
-  do {                                                                                    \
-    if (OGS_A_FULL(D, (TILE).count))                                                      \
-      warp_load_state<MODE, D, true>(m.b[D], TILE, m.wemask, TI, use_mask, pat, lane, S); \
-    else                                                                                  \
-      warp_load_state<MODE, D>(m.b[D], TILE, m.wemask, TI, use_mask, pat, lane, S);       \
-  } while (0)
+#define OGS_A_LOAD(D, TILE, TI, S) warp_load_state<MODE, D>(m.b[D], TILE, m.wemask, TI, use_mask, pat, lane, S)
 #define OGS_A_LOAD_CUR(D) OGS_A_LOAD(D, cur, tcur, scur)
   OGS_DEGREE_SWITCH(cur.bucket, OGS_A_LOAD_CUR)
 #undef OGS_A_LOAD_CUR
@@ -184,13 +155,7 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
   {
     const int k0 = comp_of(i);
     const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, k0);
-#define OGS_A_ISSUE0(D)                                                                      \
-  do {                                                                                       \
-    if (OGS_A_FULL(D, scur.cnt))                                                             \
-      async_issue_vals<T, MODE, D, true>(scur, src, gv, stride, K, k0, gmask, lane, ring);   \
-    else                                                                                     \
-      async_issue_vals<T, MODE, D>(scur, src, gv, stride, K, k0, gmask, lane, ring);         \
-  } while (0)
+#define OGS_A_ISSUE0(D) async_issue_vals<T, MODE, D>(scur, src, gv, stride, K, k0, gmask, lane, ring)
     OGS_DEGREE_SWITCH(cur.bucket, OGS_A_ISSUE0)
 #undef OGS_A_ISSUE0
   }
@@ -205,13 +170,7 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
       const int k1 = comp_of(i + W);
       const T* src1 = (MODE == kModeScatter) ? nullptr : field_base<T>(f, k1);
       T* st1 = ring + nstage * (kWarpSlots * 32);
-#define OGS_A_ISSUE1(D)                                                                      \
-  do {                                                                                       \
-    if (OGS_A_FULL(D, snxt.cnt))                                                             \
-      async_issue_vals<T, MODE, D, true>(snxt, src1, gv, stride, K, k1, gmask, lane, st1);   \
-    else                                                                                     \
-      async_issue_vals<T, MODE, D>(snxt, src1, gv, stride, K, k1, gmask, lane, st1);         \
-  } while (0)
+#define OGS_A_ISSUE1(D) async_issue_vals<T, MODE, D>(snxt, src1, gv, stride, K, k1, gmask, lane, st1)
       OGS_DEGREE_SWITCH(nxt.bucket, OGS_A_ISSUE1)
 #undef OGS_A_ISSUE1
     }
@@ -232,15 +191,10 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
       T* dst = (MODE == kModeGather) ? nullptr : field_base<T>(f, k0);
       const T* st0 = ring + stage * (kWarpSlots * 32);
       T V[kWarpSlots];
-#define OGS_A_FOLD(D)                                                                                \
-  do {                                                                                               \
-    if (OGS_A_FULL(D, scur.cnt)) {                                                                   \
-      async_read_vals<T, MODE, D, true>(scur, gmask, lane, st0, V);                                  \
-      warp_fold_store<T, OP, MODE, D, true>(scur, dst, gv, stride, K, k0, gmask, smode, gslib, lane, V); \
-    } else {                                                                                         \
-      async_read_vals<T, MODE, D>(scur, gmask, lane, st0, V);                                        \
-      warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, k0, gmask, smode, gslib, lane, V);   \
-    }                                                                                                \
+#define OGS_A_FOLD(D)                                                                            \
+  do {                                                                                           \
+    async_read_vals<T, MODE, D>(scur, gmask, lane, st0, V);                                      \
+    warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, k0, gmask, smode, gslib, lane, V); \
   } while (0)
       OGS_DEGREE_SWITCH(cur.bucket, OGS_A_FOLD)
 #undef OGS_A_FOLD
@@ -258,7 +212,6 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
   }
   cp_async_wait<0>();
 #undef OGS_A_LOAD
-#undef OGS_A_FULL
 }
 
 template <typename T, int OP, int MODE, int KL, bool PLAIN>

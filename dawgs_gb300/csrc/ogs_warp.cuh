@@ -60,19 +60,17 @@ struct WarpState {
   int32_t cnt;              // rows of the tile this call processes
 };
 
-// FULL: the caller knows that the tile holds warp_rows_per_tile(D) rows and
-// that no row limit applies, so the per-row bounds checks drop out.
-template <int MODE, int D, bool FULL = false>
+template <int MODE, int D>
 __device__ __forceinline__ void warp_load_state(const DevBucket& b, const Tile& t, const uint8_t* wemask,
                                                 int tile_index, bool use_mask, const Pattern& pat, int lane,
                                                 WarpState& s) {
   constexpr int RPT = warp_rows_per_lane(D);
-  s.cnt = FULL ? warp_rows_per_tile(D) : (pat.limit_n ? min(t.count, b.nP - t.begin) : t.count);
+  s.cnt = pat.limit_n ? min(t.count, b.nP - t.begin) : t.count;
   s.emask = use_mask ? __ldg(wemask + static_cast<int64_t>(tile_index) * 32 + lane) : 0xFFu;
 #pragma unroll
   for (int j = 0; j < RPT; ++j) {
     const int r = j * 32 + lane;
-    if (FULL || r < s.cnt) {
+    if (r < s.cnt) {
       const int idx = t.begin + r;
 #pragma unroll
       for (int q = 0; q < D; ++q) s.I[j * D + q] = __ldg(b.cols + static_cast<int64_t>(q) * b.stride + idx);
@@ -102,14 +100,14 @@ __device__ __forceinline__ void warp_load_vals(const WarpState& s, const T* src,
 // smode: 0 write every member, 1 only N members, 2 N members or, in a row
 // without any, member 0 (gslib transpose 1).  gslib: fold from the first
 // member taking part instead of from the identity (gs_local.c:58-72).
-template <typename T, int OP, int MODE, int D, bool FULL = false>
+template <typename T, int OP, int MODE, int D>
 __device__ __forceinline__ void warp_fold_store(const WarpState& s, T* dst, T* gv, int64_t stride, int K, int k,
                                                 bool gmask, int smode, bool gslib, int lane,
                                                 const T (&V)[kWarpSlots]) {
   constexpr int RPT = warp_rows_per_lane(D);
 #pragma unroll
   for (int j = 0; j < RPT; ++j) {
-    if (FULL || j * 32 + lane < s.cnt) {
+    if (j * 32 + lane < s.cnt) {
       T a;
       if (MODE == kModeScatter) {
         a = V[j];
