@@ -223,17 +223,31 @@ def run_batched(a, dev, L, stream, log=None):
     batch = ogs.ogs_batch_t([(g, f, k, ogs.Add, ogs.Sym) for g, f, k in zip(handles, fields, ks)], graph=True)
     grid = batch.tune(stream)
 
-    def time_it(fn, reps):
+    def restore():
+        for f, p0 in zip(fields, pristine):
+            f.copy_(p0)
+
+    def time_it(fn, reps, chunk=50):
+        # Repeated Add GatherScatter on one field multiplies a degree-d row by
+        # d per call: within a few hundred calls the high-degree rows reach
+        # +-inf and their stores turn silent.  The fields are restored every
+        # `chunk` calls, outside the timed windows.
+        restore()
         for _ in range(3):
             fn()
-        torch.cuda.synchronize(dev)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(reps):
-            fn()
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        return e0.elapsed_time(e1) * 1e-3 / reps
+        total, done = 0.0, 0
+        while done < reps:
+            n = min(chunk, reps - done)
+            restore()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(n):
+                fn()
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            total += e0.elapsed_time(e1) * 1e-3
+            done += n
+        return total / reps
 
     def plain():
         for g, f, k in zip(handles, fields, ks):
@@ -242,12 +256,10 @@ def run_batched(a, dev, L, stream, log=None):
     t_plain = time_it(plain, max(a.steps // 2, 5))
     t_batch = time_it(lambda: batch.GatherScatter(stream), max(a.steps, 10))
     # results: batched equals plain bit for bit (both from the pristine fields)
-    for f, p0 in zip(fields, pristine):
-        f.copy_(p0)
+    restore()
     batch.GatherScatter(stream)
     got = [f.clone() for f in fields]
-    for f, p0 in zip(fields, pristine):
-        f.copy_(p0)
+    restore()
     plain()
     torch.cuda.synchronize(dev)
     same = all(torch.equal(x, y) for x, y in zip(got, fields))
@@ -515,11 +527,16 @@ def run_ours(a):
     # warm: back-to-back calls on one field, no flush and no restore, so the
     # column ids and the field stay in L2 between calls (reported beside the
     # cold headline, not instead of it)
+    # (the field is restored every 100 calls, outside the timed calls: repeated
+    # Add multiplies a degree-d row by d per call, and rows that reached +-inf
+    # would turn their stores silent)
     wev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
     work.copy_(pristine)
     for _ in range(3):
         step()
-    for e0, e1 in wev:
+    for j, (e0, e1) in enumerate(wev):
+        if j % 100 == 0:
+            work.copy_(pristine)
         step(e0, e1)
     torch.cuda.synchronize(dev)
     warm_per_step = sum(e0.elapsed_time(e1) * 1e-3 for e0, e1 in wev) / a.steps
