@@ -274,9 +274,12 @@ def run_batched(a, dev, L, stream, log=None):
 def run_served(a, dev, L, stream):
     """Served gather-scatter: 64 resident meshes drawn like the batched mix; a
     request picks a mesh uniformly, fp64 or fp32 (50/50), k uniform in [1,8],
-    op Add 80% / Min 10% / Max 10%, values U[-1,1] (integers are not used);
-    fields live in pinned host memory and are admitted against a 16 GB device
-    budget.  First a saturation run (all requests queued at once) gives the
+    op Add 80% / Min 10% / Max 10% (integers are not used); fields are slices
+    of one pinned host arena, initialised U[-1,1] and reused round-robin, so a
+    later request finds what earlier ones left there (after many repeated Adds
+    that includes +-inf and NaN bit patterns): this leg measures throughput and
+    latency, the per-request results are checked by the served tests.
+    Requests are admitted against a 16 GB device budget.  First a saturation run (all requests queued at once) gives the
     throughput; then Poisson arrivals at 25%, 50% and 80% of it give p50/p99
     latency, counted from each request's scheduled arrival.  Plain = the same
     requests one after another through ogs_gather_scatter_host."""
