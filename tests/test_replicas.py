@@ -33,7 +33,7 @@ def _rank(rank, world, port, out):
 
 def test_aggregate_over_two_gloo_ranks():
     world = 2
-    out = mp.Manager().dict()
+    out = mp.get_context("spawn").Manager().dict()
     mp.spawn(_rank, args=(world, _free_port(), out), nprocs=world, join=True)
     for r in range(world):
         t, u, thr = out[r]
