@@ -692,10 +692,17 @@ def run_sweep(a):
     tcode = {torch.float64: 1, torch.float32: 0, torch.int32: 2, torch.int64: 3}
     reps = max(a.steps, 5)
 
-    def timeit(fn, restore=None, cold=True):
-        ts = []
+    def timeit(fn, restore=None, cold=True, restore_every=1):
+        # restore_every > 1 (warm figures): the field goes back to its start
+        # every few calls, untimed, so that repeated Add cannot drive rows to
+        # +-inf (stores of rows already at inf are silent)
+        # The calls are queued back to back and synchronised once at the end:
+        # with a synchronisation between calls the GPU would sit idle from the
+        # start event until the host's launch arrives, and the event pair
+        # would time the host call too.
+        evs = []
         for i in range(reps + 3):
-            if restore is not None:
+            if restore is not None and i % restore_every == 0:
                 restore()
             if cold:
                 flush.zero_()
@@ -704,11 +711,12 @@ def run_sweep(a):
             e0.record(st)
             rc = fn()
             e1.record(st)
-            torch.cuda.synchronize(dev)
             if rc:
                 raise SystemExit(f"bench --sweep: status {rc}: {L.ogs_last_error_string().decode()}")
             if i >= 3:
-                ts.append(e0.elapsed_time(e1) * 1e-3)
+                evs.append((e0, e1))
+        torch.cuda.synchronize(dev)
+        ts = [e0.elapsed_time(e1) * 1e-3 for e0, e1 in evs]
         # CUDA event times come in steps of about 1 us on GB300: a median of
         # quantised samples is off by up to a step, the mean of the middle 80 %
         # of many samples is not
@@ -739,7 +747,12 @@ def run_sweep(a):
                 for m, q in zip(many, m0):
                     m.copy_(q)
             t = timeit(fn, restore=restore)
-        warm = timeit(fn, cold=False) if op == 0 else None
+        if op != 0:
+            warm = None
+        elif many is None:
+            warm = timeit(fn, restore=lambda: x.copy_(x0), cold=False, restore_every=50)
+        else:
+            warm = timeit(fn, restore=restore, cold=False, restore_every=50)
         emit(case, g, k, t, ab, warm)
 
     def idx_bytes(g):
@@ -751,7 +764,10 @@ def run_sweep(a):
         x = torch.from_numpy(mesh.uniform_values(ids.size, np.float64, -1, 1, p)).to(dev)
         gs(f"24^3 p={p} f64 Add GS", g, x, 1, 0, 16 * ids.size + idx_bytes(g))
         if p == 7:
-            gs("24^3 p=7 f32 Add GS", g, x.float(), 1, 0, 8 * ids.size + idx_bytes(g))
+            # every case below starts from fresh seeded values, not from a field
+            # that earlier timings have already folded
+            xf = torch.from_numpy(mesh.uniform_values(ids.size, np.float32, -1, 1, p)).to(dev)
+            gs("24^3 p=7 f32 Add GS", g, xf, 1, 0, 8 * ids.size + idx_bytes(g))
             for dt in (torch.int32, torch.int64):
                 xi = torch.from_numpy(mesh.uniform_values(ids.size, np.int64, -(2 ** 30), 2 ** 30, 3)).to(dev).to(dt)
                 for op, nm in ((3, "Min"), (2, "Max")):
@@ -762,6 +778,7 @@ def run_sweep(a):
             sa = ids.copy()
             sg = ogs.ogs_t().Setup(sa.size, sa, None, ogs.Signed, ogs.Auto, True)
             gv = torch.zeros(sg.Ngather, dtype=torch.float64, device=dev)
+            x = torch.from_numpy(mesh.uniform_values(ids.size, np.float64, -1, 1, p)).to(dev)
             abg = 8 * (ids.size + sg.Ngather) + idx_bytes(sg)
             for nm, fn in (("Gather Trans", lambda: L.ogs_gather(sg.handle, gv.data_ptr(), x.data_ptr(), 1, 1, 0, 2,
                                                                  st.cuda_stream)),
