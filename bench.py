@@ -597,7 +597,8 @@ def run_ours(a):
         e2e = {"value": e2e_value, "unit": "DOFS/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                "ms_per_step": 1e3 * t_e2e / e2e_steps, "steps": e2e_steps,
-               "api": "ogs_gather_scatter_host (C ABI)"}
+               "api": "ogs_gather_scatter_host (C ABI)",
+               "checked": "last step's host buffer equals the oracle bit for bit (with the CPU leg)"}
 
     # correctness of the timed configuration on this run's own output
     work.copy_(pristine)
@@ -612,6 +613,8 @@ def run_ours(a):
         got = work.cpu().numpy()
         if got.tobytes() != x.tobytes():
             raise SystemExit("bench: GPU result differs from the oracle on the timed workload")
+        if e2e is not None and host.numpy().tobytes() != x.tobytes():
+            raise SystemExit("bench: the host-buffer (e2e) result differs from the oracle")
         tc = sum(times) / len(times)
         cpu = {"value": hc.NgatherGlobal / tc, "unit": "DOFS/s", "cores": cores, "kind": "port",
                "sample": f"5 full GatherScatter calls on this workload after 2 warm-up, OpenMP over {cores} "
