@@ -51,6 +51,10 @@ def test_rejects_invalid_setups(built_lib):
     assert _setup(ids, kind=7)[0] == _lib.OGS_EINVAL
     bad = np.array([1, -(2 ** 63), 3], np.int64)
     assert _setup(bad)[0] == _lib.OGS_ERANGE
+    # device indices are 32-bit (dlong = int, types.h:59-63): N is checked before ids are read
+    h0 = C.c_void_p()
+    assert built_lib.ogs_setup_ex(C.byref(h0), 2 ** 31, ids.ctypes.data, 0, 0, _lib.SETUP_HOST_ONLY) == \
+        _lib.OGS_ERANGE
     h = C.c_void_p()
     assert built_lib.ogs_setup_ex(C.byref(h), -1, None, 0, 0, _lib.SETUP_HOST_ONLY) == _lib.OGS_EINVAL
     assert built_lib.ogs_setup_ex(C.byref(h), 5, None, 0, 0, _lib.SETUP_HOST_ONLY) == _lib.OGS_EINVAL
