@@ -42,6 +42,7 @@ SIGNATURES = {
     "ogs_get_counts": (_i, [_vp, _vp]),
     "ogs_get_maps": (_i, [_vp, _vp, _vp, _vp, _vp]),
     "ogs_get_layout_stats": (_i, [_vp, _vp]),
+    "ogs_checked_id_errors": (_i, [_vp, _vp]),
     "ogs_gslib_setup": (_i, [C.POINTER(_vp), _vp, _i64, _u]),
     "ogs_gslib_gs": (_i, [_vp, _vp, _i, _i, _i, _vp]),
     "ogs_gslib_gs_vec": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),

@@ -83,9 +83,12 @@ __device__ __forceinline__ void batch_load_state(const BatchItem& it, int lane, 
   b.cols = it.cols;
   b.rows = nullptr;
   b.nmask = nullptr;
-  b.n = 0;
+  b.n = INT32_MAX;  // the records carry no bucket sizes: batched launches are not id-checked
   b.nP = it.nP;
   b.stride = it.stride;
+  b.nnodes = INT32_MAX;
+  b.nrows = INT32_MAX;
+  b.err = nullptr;
   Tile t;
   t.begin = it.begin;
   t.count = it.bucket_count & 0xFFFF;

@@ -524,6 +524,17 @@ ogs_status ogs_get_maps(ogs_handle h, int32_t* rowStartsT, int32_t* colIdsT, int
   return OGS_OK;
 }
 
+ogs_status ogs_checked_id_errors(ogs_handle h, uint64_t* count) {
+  if (!h || !count) return set_error(OGS_EINVAL, "ogs_checked_id_errors: NULL argument");
+  *count = 0;
+  if (h->host_only || !h->arena || !h->dmaps.b[1].err) return OGS_OK;
+  unsigned int v = 0;
+  const cudaError_t e = cudaMemcpy(&v, h->dmaps.b[1].err, sizeof(v), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_status(e, "ogs_checked_id_errors", "copy");
+  *count = v;
+  return OGS_OK;
+}
+
 ogs_status ogs_get_layout_stats(ogs_handle h, ogs_layout_stats* out) {
   if (!h || !out) return set_error(OGS_EINVAL, "ogs_get_layout_stats: NULL argument");
   std::memset(out, 0, sizeof(*out));

@@ -536,6 +536,7 @@ ogs_status build_device_layout(ogs_handle_s* h, const int32_t* rsT, const int32_
   const size_t o_wtiles = add(L.wtiles.size() * sizeof(Tile));
   const size_t o_wemask = add(sgn ? L.wtiles.size() * 32 : 0);
   const size_t o_wrecs = add(L.wtiles.size() * sizeof(WarpRec));
+  const size_t o_err = add(sizeof(uint32_t));  // ids out of range (checked builds); zeroed with the arena
   int dev = 0;
   if ((e = cudaGetDevice(&dev))) return fail(e, "device");
   char* base = nullptr;
@@ -636,6 +637,7 @@ ogs_status build_device_layout(ogs_handle_s* h, const int32_t* rsT, const int32_
   m.wemask = reinterpret_cast<const uint8_t*>(base + o_wemask);
   m.wrecs = reinterpret_cast<const WarpRec*>(base + o_wrecs);
   m.signed_maps = sgn ? 1 : 0;
+  set_id_bounds(h, m, reinterpret_cast<unsigned int*>(base + o_err));
   return OGS_OK;
 }
 

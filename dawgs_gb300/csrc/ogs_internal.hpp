@@ -37,6 +37,15 @@ struct DeviceCache {
   }
 };
 
+// Checked builds (-DOGS_CHECK_BOUNDS=1, for tests): every column id and row
+// id a kernel loads from the maps is compared with the handle's node and row
+// counts before a value is read or written through it; an id out of range
+// is counted in the handle's error word and replaced by 0, so the access
+// stays inside the field.  Default builds compile the checks out.
+#ifndef OGS_CHECK_BOUNDS
+#define OGS_CHECK_BOUNDS 0
+#endif
+
 // Rows of exact degree 1..kDmax are stored in fixed-width buckets; rows of a
 // larger degree go to one general CSR bucket.
 constexpr int kDmax = 8;
@@ -96,6 +105,9 @@ struct DevBucket {
   int32_t n;             // rows in the bucket
   int32_t nP;            // rows with row id < NrowsN, a prefix of the bucket
   int32_t stride;        // n rounded up to a multiple of 4
+  int32_t nnodes;        // local nodes: column ids lie in [0, nnodes)
+  int32_t nrows;         // rows of the T map: row ids lie in [0, nrows)
+  unsigned int* err;     // ids found out of range (checked builds); may be null
 };
 
 // Rows of degree > kDmax, CSR relative to the bucket.
@@ -106,6 +118,8 @@ struct DevGeneral {
   const int32_t* startsN;  // [n+1] (alias startsT when Unsigned)
   const int32_t* colsN;
   int32_t n, nP;
+  int32_t nnodes, nrows;   // as in DevBucket
+  unsigned int* err;
 };
 
 // A tile: `count` consecutive rows of one bucket, starting at `begin`.
@@ -262,6 +276,8 @@ ogs_status build_device_layout(ogs_handle_s* h, const int32_t* d_rsT, const int3
                                const int32_t* d_ciN, void* stream);
 // DevMaps restricted to the tiles of one phase.
 DevMaps phase_maps(const DevMaps& m, const Phase& p);
+// The id ranges and error word of every bucket (both setup paths).
+void set_id_bounds(const ogs_handle_s* h, DevMaps& m, unsigned int* err);
 
 // Per-type launchers (ogs_kern_*.cu).  Return a cudaError_t value.  k = 1
 // interleaved fields take the pipelined kernel over the exact-degree tiles

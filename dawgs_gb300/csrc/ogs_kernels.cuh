@@ -26,6 +26,21 @@
 
 namespace ogsgb {
 
+// A column or row id loaded from the maps, checked against [0, lim) in
+// checked builds: an id outside is counted in *err and replaced by 0.
+__device__ __forceinline__ int32_t checked_id(int32_t id, int32_t lim, unsigned int* err) {
+#if OGS_CHECK_BOUNDS
+  if (static_cast<uint32_t>(id) >= static_cast<uint32_t>(lim)) {
+    if (err) atomicAdd(err, 1u);
+    return 0;
+  }
+#else
+  (void)lim;
+  (void)err;
+#endif
+  return id;
+}
+
 template <typename T>
 __device__ __forceinline__ T type_max() {
   if constexpr (std::is_same<T, float>::value) return FLT_MAX;
@@ -99,6 +114,7 @@ __device__ __forceinline__ void run_fixed(const DevBucket& b, const Tile& t, con
   for (int j = 0; j < RPT; ++j) {
     idx[j] = t.begin + static_cast<int>(threadIdx.x) + j * kBlock;
     ok[j] = idx[j] < end;
+    if (OGS_CHECK_BOUNDS && ok[j] && idx[j] >= b.n) ok[j] = checked_id(idx[j], b.n, b.err) != 0;
   }
 #pragma unroll
   for (int j = 0; j < RPT; ++j) {
@@ -106,9 +122,9 @@ __device__ __forceinline__ void run_fixed(const DevBucket& b, const Tile& t, con
     row[j] = 0;
     if (ok[j]) {
 #pragma unroll
-      for (int m = 0; m < D; ++m) c[j][m] = __ldg(b.cols + m * n + idx[j]);
+      for (int m = 0; m < D; ++m) c[j][m] = checked_id(__ldg(b.cols + m * n + idx[j]), b.nnodes, b.err);
       if (use_mask) msk[j] = __ldg(b.nmask + idx[j]);
-      if (MODE != kModeGS) row[j] = __ldg(b.rows + idx[j]);
+      if (MODE != kModeGS) row[j] = checked_id(__ldg(b.rows + idx[j]), b.nrows, b.err);
     }
   }
   const uint32_t gmask_on = pat.gather_n ? 1u : 0u;
@@ -174,7 +190,7 @@ __device__ __forceinline__ void run_general(const DevGeneral& g, const Tile& t, 
   const int32_t* sc = pat.scatter_n ? g.colsN : g.colsT;
   const int32_t* ss = pat.scatter_n ? g.startsN : g.startsT;
   const int32_t g0 = gs[i], g1 = gs[i + 1], s0 = ss[i], s1 = ss[i + 1];
-  const int64_t r = (MODE != kModeGS) ? g.rows[i] : 0;
+  const int64_t r = (MODE != kModeGS) ? checked_id(g.rows[i], g.nrows, g.err) : 0;
   const int K = K1 ? 1 : f.K;
   const int64_t stride = K1 ? 1 : (f.is_many ? 1 : K);
   for (int k = 0; k < K; ++k) {
@@ -185,24 +201,27 @@ __device__ __forceinline__ void run_general(const DevGeneral& g, const Tile& t, 
       // gslib: fold from the first member taking part (gs_local.c:58-72)
       const T* src = field_base<T>(f, k);
       if (g1 > g0) {
-        a = src[static_cast<int64_t>(gc[g0]) * stride];
-        for (int32_t q = g0 + 1; q < g1; ++q) op_apply<T, OP>(a, src[static_cast<int64_t>(gc[q]) * stride]);
+        a = src[static_cast<int64_t>(checked_id(gc[g0], g.nnodes, g.err)) * stride];
+        for (int32_t q = g0 + 1; q < g1; ++q)
+          op_apply<T, OP>(a, src[static_cast<int64_t>(checked_id(gc[q], g.nnodes, g.err)) * stride]);
       } else {
         a = op_init_gs<T, OP>();
       }
     } else {
       const T* src = field_base<T>(f, k);
       a = op_init<T, OP>();
-      for (int32_t q = g0; q < g1; ++q) op_apply<T, OP>(a, src[static_cast<int64_t>(gc[q]) * stride]);
+      for (int32_t q = g0; q < g1; ++q)
+        op_apply<T, OP>(a, src[static_cast<int64_t>(checked_id(gc[q], g.nnodes, g.err)) * stride]);
     }
     if (MODE == kModeGather) {
       static_cast<T*>(f.gv)[r * K + k] = a;
     } else {
       T* dst = field_base<T>(f, k);
       if (pat.scatter_n == 2 && g.startsN[i + 1] == g.startsN[i]) {
-        dst[static_cast<int64_t>(g.colsT[g.startsT[i]]) * stride] = a;  // no unflagged member: the primary only
+        // no unflagged member: the primary only
+        dst[static_cast<int64_t>(checked_id(g.colsT[g.startsT[i]], g.nnodes, g.err)) * stride] = a;
       } else {
-        for (int32_t q = s0; q < s1; ++q) dst[static_cast<int64_t>(sc[q]) * stride] = a;
+        for (int32_t q = s0; q < s1; ++q) dst[static_cast<int64_t>(checked_id(sc[q], g.nnodes, g.err)) * stride] = a;
       }
     }
   }

@@ -400,6 +400,17 @@ void build_phases(ogs_handle_s* h, int max_phases) {
   }
 }
 
+void set_id_bounds(const ogs_handle_s* h, DevMaps& m, unsigned int* err) {
+  for (int d = 1; d <= kDmax; ++d) {
+    m.b[d].nnodes = static_cast<int32_t>(h->N);
+    m.b[d].nrows = static_cast<int32_t>(h->NlocalT);
+    m.b[d].err = err;
+  }
+  m.g.nnodes = static_cast<int32_t>(h->N);
+  m.g.nrows = static_cast<int32_t>(h->NlocalT);
+  m.g.err = err;
+}
+
 DevMaps phase_maps(const DevMaps& m, const Phase& p) {
   DevMaps r = m;
   r.wtiles = m.wtiles + p.w0;
@@ -459,6 +470,8 @@ ogs_status upload_layout(ogs_handle_s* h) {
   // warp records hold device pointers: filled in once the arena exists
   std::vector<WarpRec> wrecs(L.wtiles.size());
   const size_t o_wrecs = add(wrecs.data(), wrecs.size() * sizeof(WarpRec));
+  const uint32_t zero = 0;
+  const size_t o_err = add(&zero, sizeof(zero));  // ids out of range (checked builds)
 
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -516,6 +529,7 @@ ogs_status upload_layout(ogs_handle_s* h) {
   m.nwtiles = static_cast<int32_t>(L.wtiles.size());
   m.wemask = reinterpret_cast<const uint8_t*>(base + o_wemask);
   m.wrecs = reinterpret_cast<const WarpRec*>(base + o_wrecs);
+  set_id_bounds(h, m, reinterpret_cast<unsigned int*>(base + o_err));
 
   m.signed_maps = sgn ? 1 : 0;
   return OGS_OK;

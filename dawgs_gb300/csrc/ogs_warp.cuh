@@ -71,10 +71,12 @@ __device__ __forceinline__ void warp_load_state(const DevBucket& b, const Tile& 
   for (int j = 0; j < RPT; ++j) {
     const int r = j * 32 + lane;
     if (r < s.cnt) {
-      const int idx = t.begin + r;
+      // (checked builds) a tile reaching past its bucket reads bucket row 0
+      const int idx = OGS_CHECK_BOUNDS ? checked_id(t.begin + r, b.n, b.err) : t.begin + r;
 #pragma unroll
-      for (int q = 0; q < D; ++q) s.I[j * D + q] = __ldg(b.cols + static_cast<int64_t>(q) * b.stride + idx);
-      if (MODE != kModeGS) s.R[j] = __ldg(b.rows + idx);
+      for (int q = 0; q < D; ++q)
+        s.I[j * D + q] = checked_id(__ldg(b.cols + static_cast<int64_t>(q) * b.stride + idx), b.nnodes, b.err);
+      if (MODE != kModeGS) s.R[j] = checked_id(__ldg(b.rows + idx), b.nrows, b.err);
     }
   }
 }

@@ -262,6 +262,12 @@ class ogs_t:
                                  ciN.ctypes.data))
         return rsT, ciT[: self.nnzT], rsN, ciN[: self.nnzN]
 
+    def checked_id_errors(self) -> int:
+        """Ids out of range seen by a checked build's kernels (0 otherwise)."""
+        n = C.c_uint64()
+        check(lib().ogs_checked_id_errors(self.handle, C.byref(n)))
+        return n.value
+
     def layout_stats(self) -> dict:
         s = OgsLayoutStats()
         check(lib().ogs_get_layout_stats(self.handle, C.byref(s)))

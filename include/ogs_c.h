@@ -157,6 +157,11 @@ ogs_status ogs_get_maps(ogs_handle h, int32_t *rowStartsT, int32_t *colIdsT,
                         int32_t *rowStartsN, int32_t *colIdsN);
 /* Degree buckets and tiles the kernels run over (no reference counterpart). */
 ogs_status ogs_get_layout_stats(ogs_handle h, ogs_layout_stats *out);
+/* Column and row ids that the kernels found outside the handle's node and
+ * row ranges since setup, counted by a library built with OGS_CHECK_BOUNDS=1
+ * (a test build: each such id is replaced by 0 before any access); always 0
+ * for a default build.  Synchronises with the device. */
+ogs_status ogs_checked_id_errors(ogs_handle h, uint64_t *count);
 
 /* ---- pieces of the multi-rank path that run on the device ----
  * An operator over caller-built CSR maps: the reference's ogsOperator_t
