@@ -62,3 +62,32 @@ def test_int64_min_id_is_refused(ids, where, signed):
     with pytest.raises(ogs.OgsError):
         ogs.ogs_t().Setup(ids.size, ids.copy(), None, ogs.Signed if signed else ogs.Unsigned, ogs.Auto, False,
                           False, None, host_only=True)
+
+
+def _check_phases(ph, n):
+    """Every slice finds its nodes copied in; no later slice touches nodes
+    already copied out; the last chunks cover every node."""
+    assert ph[-1][2] == n and ph[-1][3] == n
+    prev_d = 0
+    for p, (lo, hi, h1, d1) in enumerate(ph):
+        assert hi < h1
+        assert d1 >= prev_d
+        for q in range(p + 1, len(ph)):
+            assert ph[q][0] >= d1
+        prev_d = d1
+
+
+@settings(max_examples=25, deadline=None)
+@given(st.integers(4, 12), st.integers(4, 12), st.integers(4, 10), st.integers(2, 5), st.integers(0, 2 ** 31),
+       st.booleans())
+def test_host_pipeline_slices_are_safe_on_random_boxes(nx, ny, nz, p, seed, permute):
+    """The host-buffer pipeline's slices on random box meshes, natural or
+    element-permuted, keep the copy-in / copy-out invariants."""
+    from dawgs_gb300 import mesh
+    ids = mesh.box_ids(nx, ny, nz, p)
+    if permute:
+        ids = mesh.permute_elements(ids, p, seed=seed)
+    g = ogs.ogs_t().Setup(ids.size, ids.copy(), host_only=True)
+    ph = g.layout_stats()["phases"]
+    assert 1 <= len(ph) <= 32
+    _check_phases(ph, ids.size)
