@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--dtype", choices=list(TYPE_CODE), default="float64")
     ap.add_argument("--op", choices=list(OP_CODE), default="add")
     ap.add_argument("--k", type=int, default=1)
+    ap.add_argument("--mode", choices=["gs", "gather", "scatter"], default="gs",
+                    help="the timed call: GatherScatter (Sym, Unsigned handle; the headline), or Gather (Trans) / "
+                         "Scatter (NoTrans) on a Signed unique handle, as dawgsMain.cpp:174-310 times them")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -159,13 +162,30 @@ def profiled_traffic():
     return None
 
 
+MODE_NAME = {"gs": "GatherScatter", "gather": "Gather", "scatter": "Scatter"}
+MODE_TRANS = {"gs": "Sym", "gather": "Trans", "scatter": "NoTrans"}
+
+
 def workload_name(a):
-    return f"ogs GatherScatter {a.dtype} {a.op.capitalize()} Sym k={a.k}, {a.nx}x{a.ny}x{a.nz} hex box p={a.p}"
+    mode = getattr(a, "mode", "gs")
+    op = "" if mode == "scatter" else f" {a.op.capitalize()}"
+    handle = "" if mode == "gs" else " (Signed unique handle)"
+    return (f"ogs {MODE_NAME[mode]} {a.dtype}{op} {MODE_TRANS[mode]} k={a.k}{handle}, "
+            f"{a.nx}x{a.ny}x{a.nz} hex box p={a.p}")
 
 
-def alg_bytes(N, nnz, R, k, s):
-    """GatherScatter (Sym): read and write every local value, read colIds and rowStarts."""
-    return 2 * k * s * N + 4 * nnz + 4 * (R + 1)
+def metric_name(a):
+    lead = "fp64" if a.dtype == "float64" else a.dtype
+    return f"{lead} {MODE_NAME[getattr(a, 'mode', 'gs')]} DOFS/s"
+
+
+def alg_bytes(N, nnz, R, k, s, mode="gs", Nglobal=0):
+    """GatherScatter (Sym): read and write every local value, read colIds and
+    rowStarts.  Gather / Scatter: read (write) every local value once, write
+    (read) every gathered value once, read colIds and rowStarts."""
+    if mode == "gs":
+        return 2 * k * s * N + 4 * nnz + 4 * (R + 1)
+    return k * s * (N + Nglobal) + 4 * nnz + 4 * (R + 1)
 
 
 def make_inputs(a):
@@ -182,20 +202,37 @@ def make_inputs(a):
 
 
 def cpu_reference_run(a, ids, v, warmup, steps):
-    """Oracle port of the host ogs GatherScatter on all host cores."""
+    """Oracle port of the host ogs operator of `a.mode` on all host cores:
+    GatherScatter on an Unsigned handle, or Gather (Trans) / Scatter
+    (NoTrans) on a Signed unique one (the scatter's input is the gather of v)."""
     import oracle
     oracle.build(ref=False)
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
-    h = oracle.OracleOgs(ids.copy(), "unsigned")
-    x = v.copy()
+    mode = getattr(a, "mode", "gs")
+    if mode == "gs":
+        h = oracle.OracleOgs(ids.copy(), "unsigned")
+        x = v.copy()
+        call = lambda: h.gather_scatter(x, a.k, a.op, "sym")  # noqa: E731
+        reset = lambda: np.copyto(x, v)  # noqa: E731
+    else:
+        h = oracle.OracleOgs(ids.copy(), "signed", True)
+        gv = np.zeros(a.k * h.Ngather, v.dtype)
+        h.gather(gv, v.copy(), a.k, a.op, "trans")
+        x = v.copy()
+        if mode == "gather":
+            out = np.zeros_like(gv)
+            call = lambda: h.gather(out, x, a.k, a.op, "trans")  # noqa: E731
+        else:
+            call = lambda: h.scatter(x, gv, a.k, "notrans")  # noqa: E731
+        reset = lambda: np.copyto(x, v)  # noqa: E731
     for _ in range(warmup):
-        h.gather_scatter(x, a.k, a.op, "sym")
+        call()
     times = []
     for _ in range(steps):
-        np.copyto(x, v)
+        reset()
         t0 = time.perf_counter()
-        h.gather_scatter(x, a.k, a.op, "sym")
+        call()
         times.append(time.perf_counter() - t0)
     return h, times, cores
 
@@ -442,7 +479,7 @@ def run_reference(a):
     t = sum(times) / len(times)
     value = h.NgatherGlobal / t
     line = {
-        "metric": "fp64 GatherScatter DOFS/s" if a.dtype == "float64" else f"{a.dtype} GatherScatter DOFS/s",
+        "metric": metric_name(a),
         "value": value, "unit": "DOFS/s", "impl": "reference", "n_gpus": a.gpus, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": {"float64": "f64", "float32": "f32", "int32": "i32", "int64": "i64"}[a.dtype],
@@ -450,7 +487,7 @@ def run_reference(a):
         "config": {"workload": workload_name(a), "local_dofs": int(ids.size),
                    "global_dofs": int(h.NgatherGlobal), "k": a.k, "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": value, "unit": "DOFS/s", "cores": cores, "kind": "port",
-                         "sample": f"{a.steps} full GatherScatter calls after {a.warmup} warm-up, "
+                         "sample": f"{a.steps} full {MODE_NAME[a.mode]} calls after {a.warmup} warm-up, "
                                    f"OpenMP over {cores} threads"},
         "e2e": {"value": value, "unit": "DOFS/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -472,12 +509,15 @@ def run_ours(a):
 
     from dawgs_gb300 import _lib, ogs
     ids, v = make_inputs(a)
-    g = ogs.ogs_t().Setup(ids.size, ids.copy(), None, ogs.Unsigned, ogs.Auto, False)
+    # the headline's Unsigned handle, or the Signed unique handle dawgs times
+    # Gather and Scatter on (dawgsMain.cpp:174-176)
+    kind, unique = (ogs.Unsigned, False) if a.mode == "gs" else (ogs.Signed, True)
+    g = ogs.ogs_t().Setup(ids.size, ids.copy(), None, kind, ogs.Auto, unique)
     # setup wall time, maps built on the GPU (the default at this size) and on the host
     setup_s = {"local_dofs": int(ids.size)}
     for how in ("device", "host"):
         t0 = time.perf_counter()
-        ogs.ogs_t().Setup(ids.size, ids.copy(), None, ogs.Unsigned, ogs.Auto, False, maps=how).Free()
+        ogs.ogs_t().Setup(ids.size, ids.copy(), None, kind, ogs.Auto, unique, maps=how).Free()
         setup_s[f"{how}_maps_s"] = time.perf_counter() - t0
     tcode, ocode = TYPE_CODE[a.dtype], OP_CODE[a.op]
     s = np.dtype(a.dtype).itemsize
@@ -488,11 +528,22 @@ def run_ours(a):
     stream = torch.cuda.current_stream(dev)
     L = _lib.lib()
     h = g.handle
+    # gathered vector: Gather's output, Scatter's input (the gather of the field)
+    gvd = torch.zeros(a.k * g.Ngather, dtype=pristine.dtype, device=dev)
+    if a.mode == "scatter":
+        _lib.check(L.ogs_gather(h, gvd.data_ptr(), pristine.data_ptr(), a.k, tcode, ocode, 2, stream.cuda_stream))
+
+    def call():
+        if a.mode == "gs":
+            return L.ogs_gather_scatter(h, work.data_ptr(), a.k, tcode, ocode, 0, stream.cuda_stream)
+        if a.mode == "gather":
+            return L.ogs_gather(h, gvd.data_ptr(), work.data_ptr(), a.k, tcode, ocode, 2, stream.cuda_stream)
+        return L.ogs_scatter(h, work.data_ptr(), gvd.data_ptr(), a.k, tcode, 1, stream.cuda_stream)
 
     def step(ev0=None, ev1=None):
         if ev0 is not None:
             ev0.record(stream)
-        st = L.ogs_gather_scatter(h, work.data_ptr(), a.k, tcode, ocode, 0, stream.cuda_stream)
+        st = call()
         if ev1 is not None:
             ev1.record(stream)
         if st:
@@ -547,7 +598,7 @@ def run_ours(a):
     # the reference's device algorithm (OKL gatherScatter, 512-member row
     # blocks) restated in CUDA, timed the same way on the same GPU
     refdev_line = None
-    if not a.no_refdev and rank == 0:
+    if not a.no_refdev and rank == 0 and a.mode == "gs":
         import refdev
         refdev.build()
         rd = refdev.RefDevOgs(g)
@@ -580,9 +631,21 @@ def run_ours(a):
     e2e = None
     if not a.no_e2e:
         host = torch.from_numpy(v.copy()).pin_memory()
+        host_gv = torch.zeros(a.k * g.Ngather, dtype=pristine.dtype).pin_memory()
+        if a.mode == "scatter":
+            host_gv.copy_(gvd.cpu())
+
+        def host_call():
+            if a.mode == "gs":
+                return L.ogs_gather_scatter_host(h, host.data_ptr(), a.k, tcode, ocode, 0, stream.cuda_stream)
+            if a.mode == "gather":
+                return L.ogs_gather_host(h, host_gv.data_ptr(), host.data_ptr(), a.k, tcode, ocode, 2,
+                                         stream.cuda_stream)
+            return L.ogs_scatter_host(h, host.data_ptr(), host_gv.data_ptr(), a.k, tcode, 1, stream.cuda_stream)
+
         for _ in range(3):
             host.copy_(torch.from_numpy(v))
-            _lib.check(L.ogs_gather_scatter_host(h, host.data_ptr(), a.k, tcode, ocode, 0, stream.cuda_stream))
+            _lib.check(host_call())
         et = []
         e2e_steps = min(a.steps, E2E_STEPS)
         for _ in range(e2e_steps):
@@ -590,14 +653,17 @@ def run_ours(a):
             flush_l2()
             barrier()
             t0 = time.perf_counter()
-            _lib.check(L.ogs_gather_scatter_host(h, host.data_ptr(), a.k, tcode, ocode, 0, stream.cuda_stream))
+            _lib.check(host_call())
             et.append(time.perf_counter() - t0)
         t_e2e, _, e2e_value = aggregate_over_ranks(sum(et), g.NgatherGlobal * e2e_steps, dev)
         nbytes = a.k * ids.size * s
+        gbytes = a.k * g.Ngather * s
+        h2d, d2h = {"gs": (nbytes, nbytes), "gather": (nbytes, gbytes), "scatter": (gbytes, nbytes)}[a.mode]
         e2e = {"value": e2e_value, "unit": "DOFS/s",
-               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                "ms_per_step": 1e3 * t_e2e / e2e_steps, "steps": e2e_steps,
-               "api": "ogs_gather_scatter_host (C ABI)",
+               "api": {"gs": "ogs_gather_scatter_host", "gather": "ogs_gather_host",
+                       "scatter": "ogs_scatter_host"}[a.mode] + " (C ABI)",
                "checked": "last step's host buffer equals the oracle bit for bit (with the CPU leg)"}
 
     # correctness of the timed configuration on this run's own output
@@ -609,34 +675,45 @@ def run_ours(a):
     if rank == 0 and world == 1 and not a.no_cpu:
         hc, times, cores = cpu_reference_run(a, ids, v, 2, 5)
         x = v.copy()
-        hc.gather_scatter(x, a.k, a.op, "sym")
-        got = work.cpu().numpy()
+        if a.mode == "gs":
+            hc.gather_scatter(x, a.k, a.op, "sym")
+            got, host_got = work.cpu().numpy(), (host.numpy() if e2e is not None else None)
+        elif a.mode == "gather":
+            x = np.zeros(a.k * hc.Ngather, v.dtype)
+            hc.gather(x, v.copy(), a.k, a.op, "trans")
+            got, host_got = gvd.cpu().numpy(), (host_gv.numpy() if e2e is not None else None)
+        else:
+            gx = np.zeros(a.k * hc.Ngather, v.dtype)
+            hc.gather(gx, v.copy(), a.k, a.op, "trans")
+            hc.scatter(x, gx, a.k, "notrans")
+            got, host_got = work.cpu().numpy(), (host.numpy() if e2e is not None else None)
         if got.tobytes() != x.tobytes():
             raise SystemExit("bench: GPU result differs from the oracle on the timed workload")
-        if e2e is not None and host.numpy().tobytes() != x.tobytes():
+        if host_got is not None and host_got.tobytes() != x.tobytes():
             raise SystemExit("bench: the host-buffer (e2e) result differs from the oracle")
         tc = sum(times) / len(times)
         cpu = {"value": hc.NgatherGlobal / tc, "unit": "DOFS/s", "cores": cores, "kind": "port",
-               "sample": f"5 full GatherScatter calls on this workload after 2 warm-up, OpenMP over {cores} "
-                         "threads; its output is also compared bit for bit with the GPU result"}
+               "sample": f"5 full {MODE_NAME[a.mode]} calls on this workload after 2 warm-up, OpenMP over "
+                         f"{cores} threads; its output is also compared bit for bit with the GPU result"}
 
     batched = None
-    if rank == 0 and world == 1 and not a.no_batched:
+    if rank == 0 and world == 1 and not a.no_batched and a.mode == "gs":
         batched = run_batched(a, dev, L, stream)
     served = None
-    if rank == 0 and world == 1 and not a.no_served:
+    if rank == 0 and world == 1 and not a.no_served and a.mode == "gs":
         served = run_served(a, dev, L, stream)
 
     partitioned = None
-    if rank == 0 and world == 1 and not a.no_partitioned and a.k == 1 and a.dtype == "float64" and a.op == "add":
+    if (rank == 0 and world == 1 and not a.no_partitioned and a.k == 1 and a.dtype == "float64" and a.op == "add"
+            and a.mode == "gs"):
         partitioned = run_partitioned(a, dev, stream, per_step)
 
     peak, peak_src = hbm_peak()
-    nbytes_alg = alg_bytes(ids.size, g.nnzT, g.NlocalT, a.k, s)
+    nbytes_alg = alg_bytes(ids.size, g.nnzT, g.NlocalT, a.k, s, a.mode, g.Ngather)
     achieved = nbytes_alg / per_step / 1e9
     stats = g.layout_stats()
     line = {
-        "metric": "fp64 GatherScatter DOFS/s" if a.dtype == "float64" else f"{a.dtype} GatherScatter DOFS/s",
+        "metric": metric_name(a),
         "value": value, "unit": "DOFS/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
@@ -648,7 +725,10 @@ def run_ours(a):
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "warp_tiles": stats["nwarp_tiles"], "general_tiles": stats["ngeneral_tiles"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": profiled_traffic(),
+                     "frac": achieved / peak,
+                     # the ncu capture covers the default workload only
+                     "traffic": profiled_traffic() if (a.mode, a.dtype, a.op, a.k, a.nx, a.ny, a.nz, a.p) ==
+                     ("gs", "float64", "add", 1, 24, 24, 24, 7) else None,
                      "warm": {"ms_per_step": warm_per_step * 1e3, "achieved": nbytes_alg / warm_per_step / 1e9,
                               "frac": nbytes_alg / warm_per_step / 1e9 / peak},
                      "alg_bytes_per_launch": nbytes_alg, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"

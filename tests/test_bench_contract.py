@@ -45,3 +45,27 @@ def test_our_arm_line(cuda):
     assert d["reference_device_equivalent"]["identical_results"]
     assert d["batched"]["identical_to_plain"]
     assert d["cpu_baseline"]["cores"] >= 1
+
+
+@pytest.mark.parametrize("mode", ["gather", "scatter"])
+def test_reference_arm_other_modes(built_lib, mode):
+    d = run_bench("--impl", "reference", "--mode", mode, "--steps", "3", "--warmup", "1", "--nx", "4", "--ny", "4",
+                  "--nz", "4", "--p", "2")
+    assert BASE_KEYS <= set(d)
+    assert d["metric"] == f"fp64 {mode.capitalize()} DOFS/s" and d["value"] > 0
+    assert "Signed unique" in d["config"]["workload"]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["gather", "scatter"])
+def test_our_arm_other_modes(cuda, mode):
+    """Gather (Trans) and Scatter (NoTrans) on a Signed unique handle through
+    the same harness; the GatherScatter-only legs are left out."""
+    d = run_bench("--mode", mode, "--steps", "5", "--warmup", "3", "--nx", "6", "--ny", "6", "--nz", "6", "--p", "3")
+    assert BASE_KEYS <= set(d)
+    assert d["metric"] == f"fp64 {mode.capitalize()} DOFS/s"
+    nl, ng = 6 ** 3 * 4 ** 3, 19 ** 3
+    h2d, d2h = (8 * nl, 8 * ng) if mode == "gather" else (8 * ng, 8 * nl)
+    assert (d["e2e"]["h2d_bytes_per_step"], d["e2e"]["d2h_bytes_per_step"]) == (h2d, d2h)
+    assert d["batched"] is None and d["served"] is None and d["partitioned"] is None
+    assert d["reference_device_equivalent"] is None and d["roofline"]["traffic"] is None
