@@ -77,7 +77,8 @@ class OgsCounts(C.Structure):
 class OgsLayoutStats(C.Structure):
     _fields_ = [("rows_by_degree", C.c_int64 * 9), ("nnz_general", C.c_int64),
                 ("ntiles", C.c_int64), ("device_bytes", C.c_int64), ("nphases", C.c_int64),
-                ("phases", (C.c_int64 * 4) * 32), ("nwarp_tiles", C.c_int64), ("ngeneral_tiles", C.c_int64)]
+                ("phases", (C.c_int64 * 4) * 32), ("nwarp_tiles", C.c_int64), ("ngeneral_tiles", C.c_int64),
+                ("phase_rows", (C.c_int64 * 2) * 32)]
 
 
 class OgsBatchEntry(C.Structure):

@@ -429,6 +429,87 @@ ogs_status ogs_gather_scatter_host(ogs_handle h, void* v, int k, int type, int o
   return cuda_status(cudaStreamSynchronize(st), fn, "synchronize");
 }
 
+// True when the host buffer is page-locked (the sliced pipelines need it:
+// copies of pageable memory do not overlap).
+bool host_pinned(const void* p) {
+  cudaPointerAttributes attr{};
+  const bool pinned = cudaPointerGetAttributes(&attr, p) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+  cudaGetLastError();
+  return pinned;
+}
+
+// The sliced copy/compute pipeline of the host-buffer Gather and Scatter
+// (the GatherScatter one is in ogs_gather_scatter_host).  Slice p:
+//   in  (copy_in):  Gather -- the nodes it reads [h0, h1);
+//                   Scatter -- the gathered rows it reads, up to rn, and, if
+//                   the scatter leaves some entries alone, the nodes [h0, h1);
+//   run (stream):   the slice's kernels, after its copies in;
+//   out (copy_out): Gather -- the rows final after it [r0, r1) (below nout);
+//                   Scatter -- the nodes final after it [d0, d1).
+ogs_status host_pipeline_gs_rows(ogs_handle_s* h, int mode, char* dv, char* dgv, char* hv, char* hgv,
+                                 size_t node_bytes, size_t row_bytes, int64_t nout, bool nodes_in,
+                                 const FieldArgs& f, int op, Pattern pat, int type, cudaStream_t st, const char* fn) {
+  ogs_status s;
+  if ((s = ensure_pipeline(h, fn)) != OGS_OK) return s;
+  cudaStream_t sin = static_cast<cudaStream_t>(h->copy_in);
+  cudaStream_t sout = static_cast<cudaStream_t>(h->copy_out);
+  auto ev = [&](size_t i) { return static_cast<cudaEvent_t>(h->events[i]); };
+  const std::vector<Phase>& ph = h->lay.phases;
+  const size_t P = ph.size();
+  if ((s = cuda_status(cudaEventRecord(ev(0), st), fn, "event")) != OGS_OK) return s;
+  if ((s = cuda_status(cudaStreamWaitEvent(sin, ev(0), 0), fn, "wait")) != OGS_OK) return s;
+  int64_t rows_in = 0;
+  for (size_t p = 0; p < P; ++p) {
+    if (mode == kModeGather || nodes_in) {
+      const size_t off = static_cast<size_t>(ph[p].h0) * node_bytes;
+      const size_t len = static_cast<size_t>(ph[p].h1 - ph[p].h0) * node_bytes;
+      if (len && (s = cuda_status(cudaMemcpyAsync(dv + off, hv + off, len, cudaMemcpyHostToDevice, sin), fn,
+                                  "copy in")) != OGS_OK)
+        return s;
+    }
+    if (mode == kModeScatter) {
+      const int64_t upto = std::min<int64_t>(ph[p].rn, nout);
+      if (upto > rows_in) {
+        const size_t off = static_cast<size_t>(rows_in) * row_bytes;
+        const size_t len = static_cast<size_t>(upto - rows_in) * row_bytes;
+        if ((s = cuda_status(cudaMemcpyAsync(dgv + off, hgv + off, len, cudaMemcpyHostToDevice, sin), fn,
+                             "copy in rows")) != OGS_OK)
+          return s;
+        rows_in = upto;
+      }
+    }
+    if ((s = cuda_status(cudaEventRecord(ev(1 + 2 * p), sin), fn, "event")) != OGS_OK) return s;
+  }
+  for (size_t p = 0; p < P; ++p) {
+    if ((s = cuda_status(cudaStreamWaitEvent(st, ev(1 + 2 * p), 0), fn, "wait")) != OGS_OK) return s;
+    if ((s = launch_maps(phase_maps(h->dmaps, ph[p]), f, mode, op, pat, type, st, fn)) != OGS_OK) return s;
+    if ((s = cuda_status(cudaEventRecord(ev(2 + 2 * p), st), fn, "event")) != OGS_OK) return s;
+  }
+  for (size_t p = 0; p < P; ++p) {
+    size_t off, len;
+    char *dst, *src;
+    if (mode == kModeGather) {
+      const int64_t a = std::min<int64_t>(ph[p].r0, nout), b = std::min<int64_t>(ph[p].r1, nout);
+      off = static_cast<size_t>(a) * row_bytes;
+      len = static_cast<size_t>(b - a) * row_bytes;
+      dst = hgv + off;
+      src = dgv + off;
+    } else {
+      off = static_cast<size_t>(ph[p].d0) * node_bytes;
+      len = static_cast<size_t>(ph[p].d1 - ph[p].d0) * node_bytes;
+      dst = hv + off;
+      src = dv + off;
+    }
+    if (!len) continue;
+    if ((s = cuda_status(cudaStreamWaitEvent(sout, ev(2 + 2 * p), 0), fn, "wait")) != OGS_OK) return s;
+    if ((s = cuda_status(cudaMemcpyAsync(dst, src, len, cudaMemcpyDeviceToHost, sout), fn, "copy out")) != OGS_OK)
+      return s;
+  }
+  if ((s = cuda_status(cudaStreamSynchronize(sout), fn, "synchronize")) != OGS_OK) return s;
+  if ((s = cuda_status(cudaStreamSynchronize(sin), fn, "synchronize")) != OGS_OK) return s;
+  return cuda_status(cudaStreamSynchronize(st), fn, "synchronize");
+}
+
 ogs_status ogs_gather_host(ogs_handle h, void* gv, const void* v, int k, int type, int op, int trans,
                            void* stream) {
   const char* fn = "ogs_gather_host";
@@ -445,15 +526,20 @@ ogs_status ogs_gather_host(ogs_handle h, void* gv, const void* v, int k, int typ
   if ((s = ensure_stage(h, voff + gb, fn)) != OGS_OK) return s;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   char* base = static_cast<char*>(h->stage);
-  if ((s = cuda_status(cudaMemcpyAsync(base, v, vb, cudaMemcpyHostToDevice, st), fn, "copy in")) != OGS_OK)
-    return s;
   FieldArgs f{};
   f.v = base;
   f.gv = base + voff;
   f.K = k;
+  const int64_t nout = trans == OGS_NOTRANS ? h->NlocalP : h->NlocalT;
+  if (OGS_KERNEL == 0 && h->lay.phases.size() >= 2 && host_pinned(v) && host_pinned(gv))
+    return host_pipeline_gs_rows(h, kModeGather, base, base + voff, static_cast<char*>(const_cast<void*>(v)),
+                                 static_cast<char*>(gv), static_cast<size_t>(k) * ts, static_cast<size_t>(k) * ts,
+                                 nout, true, f, op, pattern_for(h, kModeGather, trans), type, st, fn);
+  if ((s = cuda_status(cudaMemcpyAsync(base, v, vb, cudaMemcpyHostToDevice, st), fn, "copy in")) != OGS_OK)
+    return s;
   if ((s = launch(h, f, kModeGather, op, pattern_for(h, kModeGather, trans), type, stream, fn)) != OGS_OK)
     return s;
-  const size_t ob = static_cast<size_t>(trans == OGS_NOTRANS ? h->NlocalP : h->NlocalT) * k * ts;
+  const size_t ob = static_cast<size_t>(nout) * k * ts;
   if ((s = cuda_status(cudaMemcpyAsync(gv, base + voff, ob, cudaMemcpyDeviceToHost, st), fn, "copy out")) != OGS_OK)
     return s;
   return cuda_status(cudaStreamSynchronize(st), fn, "synchronize");
@@ -478,6 +564,16 @@ ogs_status ogs_scatter_host(ogs_handle h, void* v, const void* gv, int k, int ty
   // Entries outside the map keep their values, so v goes in unless the
   // scatter overwrites every entry.
   const bool writes_all = h->covers_all && !pat.scatter_n;
+  const int64_t nin = trans == OGS_TRANS ? h->NlocalP : h->NlocalT;
+  if (OGS_KERNEL == 0 && h->lay.phases.size() >= 2 && host_pinned(v) && host_pinned(gv)) {
+    FieldArgs f{};
+    f.v = base;
+    f.gv = base + voff;
+    f.K = k;
+    return host_pipeline_gs_rows(h, kModeScatter, base, base + voff, static_cast<char*>(v),
+                                 static_cast<char*>(const_cast<void*>(gv)), static_cast<size_t>(k) * ts,
+                                 static_cast<size_t>(k) * ts, nin, !writes_all, f, OGS_ADD, pat, type, st, fn);
+  }
   if (!writes_all &&
       (s = cuda_status(cudaMemcpyAsync(base, v, vb, cudaMemcpyHostToDevice, st), fn, "copy in v")) != OGS_OK)
     return s;
@@ -552,6 +648,8 @@ ogs_status ogs_get_layout_stats(ogs_handle h, ogs_layout_stats* out) {
     out->phases[p][1] = q.hi;
     out->phases[p][2] = q.h1;
     out->phases[p][3] = q.d1;
+    out->phase_rows[p][0] = q.r1;
+    out->phase_rows[p][1] = q.rn;
   }
   return OGS_OK;
 }

@@ -201,6 +201,10 @@ struct Phase {
   int32_t g0, g1;  // general tiles
   int64_t lo, hi;
   int64_t h0, h1, d0, d1;
+  // rows: the gathered vector's rows [r0, r1) are final once this slice has
+  // run (no later slice writes a row below r1); rows [0, rn) hold every row
+  // this slice or an earlier one reads (host-buffer Gather and Scatter)
+  int64_t r0, r1, rn;
 };
 
 // Host-side copy of everything built at setup.

@@ -392,11 +392,49 @@ void build_phases(ogs_handle_s* h, int max_phases) {
     final_at[p] = p == P - 1 ? fin : down(fin);
     fin = std::min(fin, L.phases[p].lo);
   }
+  // (never beyond the nodes already copied in: nodes that no row touches --
+  // zero ids -- may leave a gap between one slice's nodes and the next's,
+  // and their values must have come in before they go back out)
   int64_t prev = 0;
   for (int p = 0; p < P; ++p) {
     L.phases[p].d0 = prev;
-    L.phases[p].d1 = std::max(prev, final_at[p]);
+    L.phases[p].d1 = std::max(prev, std::min(final_at[p], L.phases[p].h1));
     prev = L.phases[p].d1;
+  }
+  // Rows.  Each row belongs to one tile and a tile's rows are >= its first
+  // row, so every row below the first row of the next slice's first tile is
+  // written by this slice or an earlier one.  A tile's rows end before the
+  // first row of the next tile of its bucket.
+  const int64_t R = h->NlocalT;
+  auto rup = [&](int64_t x) { return std::min<int64_t>(R, (x + kCopyAlignNodes - 1) / kCopyAlignNodes * kCopyAlignNodes); };
+  auto rdown = [&](int64_t x) { return x / kCopyAlignNodes * kCopyAlignNodes; };
+  std::vector<int64_t> wend(nw, R), gend(ng, R);  // one past each tile's last row
+  {
+    int32_t next_first[kDmax + 1];
+    for (int d = 0; d <= kDmax; ++d) next_first[d] = static_cast<int32_t>(R);
+    for (int32_t t = nw - 1; t >= 0; --t) {
+      const Tile& w = L.wtiles[t];
+      wend[t] = next_first[w.bucket];
+      next_first[w.bucket] = w.first_row;
+    }
+    int32_t gnext = static_cast<int32_t>(R);
+    for (int32_t t = ng - 1; t >= 0; --t) {
+      gend[t] = gnext;
+      gnext = L.gtiles[t].first_row;
+    }
+  }
+  int64_t rprev = 0, rneed = 0;
+  for (int p = 0; p < P; ++p) {
+    Phase& ph = L.phases[p];
+    int64_t later = R;  // lowest first row of any later slice's tile
+    if (ph.w1 < nw) later = std::min<int64_t>(later, L.wtiles[ph.w1].first_row);
+    if (ph.g1 < ng) later = std::min<int64_t>(later, L.gtiles[ph.g1].first_row);
+    ph.r0 = rprev;
+    ph.r1 = std::max(rprev, p == P - 1 ? R : rdown(later));
+    rprev = ph.r1;
+    for (int32_t t = ph.w0; t < ph.w1; ++t) rneed = std::max(rneed, rup(wend[t]));
+    for (int32_t t = ph.g0; t < ph.g1; ++t) rneed = std::max(rneed, rup(gend[t]));
+    ph.rn = p == P - 1 ? R : rneed;
   }
 }
 

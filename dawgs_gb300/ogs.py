@@ -275,7 +275,8 @@ class ogs_t:
                 "rows_general": int(s.rows_by_degree[0]), "nnz_general": int(s.nnz_general),
                 "ntiles": int(s.ntiles), "nwarp_tiles": int(s.nwarp_tiles),
                 "ngeneral_tiles": int(s.ngeneral_tiles), "device_bytes": int(s.device_bytes),
-                "phases": [tuple(int(x) for x in s.phases[p]) for p in range(int(s.nphases))]}
+                "phases": [tuple(int(x) for x in s.phases[p]) for p in range(int(s.nphases))],
+                "phase_rows": [tuple(int(x) for x in s.phase_rows[p]) for p in range(int(s.nphases))]}
 
 
 class ogs_batch_t:

@@ -85,6 +85,8 @@ typedef struct {
   int64_t nwarp_tiles;       /* warp tiles (32 lanes x 8 entries, exact degree): the work
                                 items of the GatherScatter/Gather/Scatter launches */
   int64_t ngeneral_tiles;    /* tiles of rows above degree 8 */
+  int64_t phase_rows[32][2]; /* per slice: end of the gathered rows final after it, end of the
+                                gathered rows it and the earlier slices read */
 } ogs_layout_stats;
 
 /* ogs_t::Setup (include/ogs.hpp:221-228; libs/ogs/ogsSetup.cpp:69-190).

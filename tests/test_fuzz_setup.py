@@ -71,6 +71,7 @@ def _check_phases(ph, n):
     prev_d = 0
     for p, (lo, hi, h1, d1) in enumerate(ph):
         assert hi < h1
+        assert d1 <= h1
         assert d1 >= prev_d
         for q in range(p + 1, len(ph)):
             assert ph[q][0] >= d1

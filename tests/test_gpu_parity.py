@@ -201,3 +201,39 @@ def test_host_pipeline_graph_replay_and_cache(cuda, oracle_mod):
             b.copy_(torch.from_numpy(v))
             g.GatherScatter(b, 1, ogs.Add, ogs.Sym)
             assert same_bits(b.numpy(), ref.gather_scatter(v.copy(), 1, "add", "sym"))
+
+
+def _zero_block(ids):
+    ids = ids.copy()
+    a = int(ids.size * 0.3)
+    ids[a:a + ids.size // 5] = 0
+    return ids
+
+
+@pytest.mark.parametrize("zero_block", [False, True])
+def test_host_gather_and_scatter_pipelines(cuda, oracle_mod, zero_block):
+    """Host-buffer Gather and Scatter on a Signed unique handle with a
+    four-slice pipeline (page-locked buffers): gathered rows go out as the
+    slices that write them finish, and the Scatter's rows come in ahead of
+    the slices that read them.  With a block of zero ids the Scatter leaves
+    those entries alone, so the field also comes in."""
+    base = mesh.box_ids(16, 14, 12, 4)
+    if zero_block:
+        base = _zero_block(base)
+    sids = signed_ids(base, seed=21)
+    a = sids.copy()
+    g = ogs.ogs_t().Setup(a.size, a, None, ogs.Signed, ogs.Auto, True)
+    assert len(g.layout_stats()["phases"]) >= 2
+    ref = oracle_mod.OracleOgs(sids.copy(), "signed", True)
+    for dtype, op in ((np.float64, "add"), (np.float32, "max"), (np.int64, "min")):
+        for trans, T in (("trans", ogs.Trans), ("notrans", ogs.NoTrans), ("sym", ogs.Sym)):
+            v = values(base.size, dtype, op, seed=31)
+            hv = torch.from_numpy(v.copy()).pin_memory()
+            hgv = torch.zeros(g.Ngather, dtype=hv.dtype).pin_memory()
+            g.Gather(hgv, hv, 1, ogs.Op[op.capitalize()], T)
+            want = ref.gather(np.zeros(g.Ngather, dtype), v.copy(), 1, op, trans)
+            assert same_bits(hgv.numpy(), want), (dtype, op, trans)
+            out = torch.from_numpy(values(base.size, dtype, op, seed=32)).pin_memory()
+            g.Scatter(out, hgv, 1, T)
+            assert same_bits(out.numpy(), ref.scatter(values(base.size, dtype, op, seed=32), want.copy(), 1, trans)), \
+                (dtype, op, trans)

@@ -77,19 +77,38 @@ def test_c2_box_counts_match_closed_form(oracle_mod):
     assert st["ngeneral_tiles"] == 0
 
 
-@pytest.mark.parametrize("name", ["c1_box", "box_permuted", "random_multiplicity", "high_degree"])
+def _box_with_zero_block():
+    ids = mesh.box_ids(16, 14, 12, 4)
+    a = int(ids.size * 0.3)
+    ids[a:a + ids.size // 5] = 0  # a block of nodes in no row, inside a four-slice pipeline
+    return ids
+
+
+PIPE_CASES = dict(CASES, box_zero_block=_box_with_zero_block, box_multi_slice=lambda: mesh.box_ids(12, 10, 9, 4))
+
+
+@pytest.mark.parametrize("name", ["c1_box", "box_permuted", "random_multiplicity", "high_degree", "box_zero_block",
+                                  "box_multi_slice"])
 def test_host_pipeline_phases_are_safe(oracle_mod, name):
     """The host-buffer pipeline copies node chunks in and out around slices of
     the tiles; every slice must find its nodes already copied in, and no later
     slice may touch nodes that were already copied out."""
-    ids = CASES[name]()
+    ids = PIPE_CASES[name]()
     g = ogs.ogs_t().Setup(ids.size, ids.copy(), host_only=True)
-    ph = g.layout_stats()["phases"]
+    st = g.layout_stats()
+    ph = st["phases"]
+    # gathered rows: the final rows grow to every row; the rows read reach every row by the last slice
+    prev_r = 0
+    for r1, rn in st["phase_rows"]:
+        assert prev_r <= r1 <= g.NlocalT and rn <= g.NlocalT
+        prev_r = r1
+    assert st["phase_rows"][-1] == (g.NlocalT, g.NlocalT)
     assert 1 <= len(ph) <= 32
     assert ph[-1][2] == ids.size and ph[-1][3] == ids.size
     prev_d = 0
     for p, (lo, hi, h1, d1) in enumerate(ph):
         assert hi < h1  # touched nodes are in chunks 0..p
+        assert d1 <= h1  # nothing goes out before it came in
         assert d1 >= prev_d
         for q in range(p + 1, len(ph)):
             assert ph[q][0] >= d1  # later slices stay above the nodes sent back
