@@ -127,7 +127,9 @@ ogs_status ogs_scatter(ogs_handle h, void *d_v, const void *d_gv, int k, int typ
  * (include/ogs.hpp:232-236, 268-273, 309-313).  The work runs on the GPU:
  * the buffers are copied to a device staging area owned by the handle, the
  * kernel runs on `stream`, results are copied back, and the call returns
- * after `stream` has synchronised.  Pinned host memory gives full copy speed. */
+ * after `stream` has synchronised.  With page-locked buffers the copies and
+ * the kernels run as a pipeline of up to 8 slices (copy in, compute and copy
+ * out overlap); pageable buffers take one copy each way. */
 ogs_status ogs_gather_scatter_host(ogs_handle h, void *v, int k, int type, int op, int trans,
                                    void *stream);
 ogs_status ogs_gather_host(ogs_handle h, void *gv, const void *v, int k, int type, int op,
