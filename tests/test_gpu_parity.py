@@ -225,15 +225,15 @@ def test_host_gather_and_scatter_pipelines(cuda, oracle_mod, zero_block):
     g = ogs.ogs_t().Setup(a.size, a, None, ogs.Signed, ogs.Auto, True)
     assert len(g.layout_stats()["phases"]) >= 2
     ref = oracle_mod.OracleOgs(sids.copy(), "signed", True)
-    for dtype, op in ((np.float64, "add"), (np.float32, "max"), (np.int64, "min")):
+    for dtype, op, k in ((np.float64, "add", 1), (np.float32, "max", 1), (np.int64, "min", 1), (np.float64, "add", 3)):
         for trans, T in (("trans", ogs.Trans), ("notrans", ogs.NoTrans), ("sym", ogs.Sym)):
-            v = values(base.size, dtype, op, seed=31)
+            v = values(k * base.size, dtype, op, seed=31)
             hv = torch.from_numpy(v.copy()).pin_memory()
-            hgv = torch.zeros(g.Ngather, dtype=hv.dtype).pin_memory()
-            g.Gather(hgv, hv, 1, ogs.Op[op.capitalize()], T)
-            want = ref.gather(np.zeros(g.Ngather, dtype), v.copy(), 1, op, trans)
-            assert same_bits(hgv.numpy(), want), (dtype, op, trans)
-            out = torch.from_numpy(values(base.size, dtype, op, seed=32)).pin_memory()
-            g.Scatter(out, hgv, 1, T)
-            assert same_bits(out.numpy(), ref.scatter(values(base.size, dtype, op, seed=32), want.copy(), 1, trans)), \
-                (dtype, op, trans)
+            hgv = torch.zeros(k * g.Ngather, dtype=hv.dtype).pin_memory()
+            g.Gather(hgv, hv, k, ogs.Op[op.capitalize()], T)
+            want = ref.gather(np.zeros(k * g.Ngather, dtype), v.copy(), k, op, trans)
+            assert same_bits(hgv.numpy(), want), (dtype, op, k, trans)
+            out = torch.from_numpy(values(k * base.size, dtype, op, seed=32)).pin_memory()
+            g.Scatter(out, hgv, k, T)
+            assert same_bits(out.numpy(), ref.scatter(values(k * base.size, dtype, op, seed=32), want.copy(), k,
+                                                      trans)), (dtype, op, k, trans)
