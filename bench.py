@@ -41,7 +41,12 @@ sys.path.insert(0, ROOT)
 # and refill the pinned buffer from the CPU: they are capped apart from the
 # kernel steps, which run long enough for several clock samples.
 E2E_STEPS = 30
-PROFILE_TRAFFIC = os.path.join(ROOT, "profiles", "ogs_async_kernel_gs_fp64_add_24x24x24_p7.md")
+# the committed ncu summaries of the default workload, per timed call
+PROFILE_TRAFFIC = {
+    "gs": os.path.join(ROOT, "profiles", "ogs_async_kernel_gs_fp64_add_24x24x24_p7.md"),
+    "gather": os.path.join(ROOT, "profiles", "ogs_async_kernel_gather_trans_fp64_24x24x24_p7.md"),
+    "scatter": os.path.join(ROOT, "profiles", "ogs_async_kernel_scatter_notrans_fp64_24x24x24_p7.md"),
+}
 FALLBACK_HBM_GBS = 6800.0
 TYPE_CODE = {"float32": 0, "float64": 1, "int32": 2, "int64": 3}
 OP_CODE = {"add": 0, "mul": 1, "max": 2, "min": 3}
@@ -151,10 +156,10 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def profiled_traffic():
+def profiled_traffic(mode="gs"):
     """dram bytes per launch from the committed ncu summary (same workload)."""
     try:
-        for line in open(PROFILE_TRAFFIC):
+        for line in open(PROFILE_TRAFFIC[mode]):
             if line.strip().startswith("dram_bytes_per_launch:"):
                 return int(line.split(":")[1].strip().replace(",", ""))
     except OSError:
@@ -727,8 +732,8 @@ def run_ours(a):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      # the ncu capture covers the default workload only
-                     "traffic": profiled_traffic() if (a.mode, a.dtype, a.op, a.k, a.nx, a.ny, a.nz, a.p) ==
-                     ("gs", "float64", "add", 1, 24, 24, 24, 7) else None,
+                     "traffic": profiled_traffic(a.mode) if (a.dtype, a.op, a.k, a.nx, a.ny, a.nz, a.p) ==
+                     ("float64", "add", 1, 24, 24, 24, 7) else None,
                      "warm": {"ms_per_step": warm_per_step * 1e3, "achieved": nbytes_alg / warm_per_step / 1e9,
                               "frac": nbytes_alg / warm_per_step / 1e9 / peak},
                      "alg_bytes_per_launch": nbytes_alg, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"
