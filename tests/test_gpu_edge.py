@@ -107,3 +107,36 @@ def test_bad_arguments_on_device_handle(cuda):
     assert L.ogs_gather_scatter(g.handle, d.data_ptr(), 1, 1, 0, 5, None) == _lib.OGS_EINVAL
     assert L.ogs_gather_scatter(g.handle, None, 1, 1, 0, 0, None) == _lib.OGS_EINVAL
 
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("op,name", [(ogs.Add, "add"), (ogs.Mul, "mul")])
+def test_nan_results_are_nan_where_the_host_has_nan(cuda, oracle_mod, dtype, op, name):
+    """Add and Mul with NaN operands or invalid steps (two different quiet
+    NaNs, a quiet then a signalling NaN, inf - inf or 0 * inf) in
+    exact-degree rows and in a row of 12 members: every entry the host makes
+    NaN is NaN here and every other entry is bit-identical.  The NaN's own
+    bits are the GPU's (fp32: 0x7fffffff; fp64: the first NaN operand, or a
+    negative quiet NaN), not the host CPU's, which differ between x86 and
+    Arm as well; following the host's rules costs the headline kernel a
+    fifth of its speed (measured), so the payload is the documented
+    deviation."""
+    ut = np.uint64 if dtype == np.float64 else np.uint32
+    qa, qb, sa = ((0x7ff8000000000123, 0xfff8000000000456, 0x7ff0000000000789) if dtype == np.float64
+                  else (0x7fc00123, 0xffc00456, 0x7f800789))
+    ids = np.array([1, 1, 2, 2, 3, 3, 4, 4, 4] + [5] * 12 + [6], np.int64)
+    g = ogs.ogs_t().Setup(ids.size, ids.copy())
+    v = np.arange(1, ids.size + 1).astype(dtype)
+    u = v.view(ut)
+    u[0], u[1], u[2], u[3] = qa, qb, qa, sa
+    if name == "add":
+        v[4], v[5] = np.inf, -np.inf
+    else:
+        v[4], v[5] = 0, np.inf
+    v[6], v[8] = -np.inf, np.inf
+    u[12], u[15] = qb, sa
+    got = gs(g, v.copy(), 1, op)
+    want = oracle_mod.OracleOgs(ids.copy(), "unsigned").gather_scatter(v.copy(), 1, name, "sym")
+    assert np.array_equal(np.isnan(got), np.isnan(want))
+    keep = ~np.isnan(want)
+    assert same_bits(got[keep], want[keep])
