@@ -92,3 +92,76 @@ def test_host_pipeline_slices_are_safe_on_random_boxes(nx, ny, nz, p, seed, perm
     ph = g.layout_stats()["phases"]
     assert 1 <= len(ph) <= 32
     _check_phases(ph, ids.size)
+
+
+@st.composite
+def _caller_maps(draw):
+    """A T map over N local nodes (rows of distinct members, ascending) and an
+    N map whose rows are subsequences of the first NrowsN T rows."""
+    N = draw(st.integers(1, 40))
+    nrows = draw(st.integers(0, 12))
+    rows = [sorted(draw(st.sets(st.integers(0, N - 1), max_size=6))) for _ in range(nrows)]
+    nrowsN = draw(st.integers(0, nrows))
+    rowsN = [sorted(draw(st.sets(st.sampled_from(r), max_size=len(r)))) if (i < nrowsN and r) else []
+             for i, r in enumerate(rows)]
+    return N, rows, nrowsN, rowsN
+
+
+def _csr(rows):
+    rs = np.zeros(len(rows) + 1, np.int32)
+    rs[1:] = np.cumsum([len(r) for r in rows])
+    ci = np.array([c for r in rows for c in r], np.int32)
+    return rs, ci
+
+
+@settings(max_examples=200, deadline=None, derandomize=True)
+@given(_caller_maps())
+def test_setup_maps_round_trip(m):
+    """Operators from caller maps (ogsOperator_t-style CSR, as the reference's
+    setup builds gatherLocal / gatherHalo / postmpi) keep the maps exactly."""
+    N, rows, nrowsN, rowsN = m
+    rsT, ciT = _csr(rows)
+    rsN, ciN = _csr(rowsN)
+    g = ogs.ogs_t().SetupMaps(N, rsT, ciT, rsN, ciN, NrowsN=nrowsN, host_only=True)
+    assert (g.N, g.NlocalT, g.NlocalP, g.nnzT, g.nnzN) == (N, len(rows), nrowsN, ciT.size, ciN.size)
+    got = g.maps()
+    assert np.array_equal(got[0], rsT) and np.array_equal(got[1], ciT)
+    assert np.array_equal(got[2], rsN) and np.array_equal(got[3], ciN)
+    stats = g.layout_stats()
+    deg = np.diff(rsT)
+    assert sum(stats["rows_by_degree"].values()) + stats["rows_general"] == len(rows)
+    for d, n in stats["rows_by_degree"].items():
+        assert n == int((deg == d).sum())
+
+
+@settings(max_examples=100, deadline=None, derandomize=True)
+@given(_caller_maps(), st.integers(0, 2))
+def test_setup_maps_refuses_broken_maps(m, how):
+    """A column outside [0, N), an N member missing from its T row, or an N
+    row at or above NrowsN is refused."""
+    N, rows, nrowsN, rowsN = m
+    rsT, ciT = _csr(rows)
+    rsN, ciN = _csr(rowsN)
+    if how == 0:
+        if ciT.size == 0:
+            return
+        ciT = ciT.copy()
+        ciT[-1] = N  # outside [0, N)
+    elif how == 1:
+        cand = [i for i in range(nrowsN) if len(rows[i]) < N]
+        if not cand:
+            return
+        i = cand[0]
+        missing = next(c for c in range(N) if c not in rows[i])
+        rowsN = [list(r) for r in rowsN]
+        rowsN[i] = sorted(set(rowsN[i]) | {missing})
+        rsN, ciN = _csr(rowsN)
+    else:
+        j = next((i for i in range(nrowsN, len(rows)) if rows[i]), None)
+        if j is None:
+            return
+        rowsN = [list(r) for r in rowsN]
+        rowsN[j] = [rows[j][0]]
+        rsN, ciN = _csr(rowsN)
+    with pytest.raises(ogs.OgsError):
+        ogs.ogs_t().SetupMaps(N, rsT, ciT, rsN, ciN, NrowsN=nrowsN, host_only=True)
