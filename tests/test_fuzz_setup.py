@@ -165,3 +165,19 @@ def test_setup_maps_refuses_broken_maps(m, how):
         rsN, ciN = _csr(rowsN)
     with pytest.raises(ogs.OgsError):
         ogs.ogs_t().SetupMaps(N, rsT, ciT, rsN, ciN, NrowsN=nrowsN, host_only=True)
+
+
+@settings(max_examples=40, deadline=None, derandomize=True)
+@given(st.integers(1, 7), st.integers(1, 7), st.integers(1, 7), st.integers(1, 6), st.booleans(), st.integers(0, 99))
+def test_box_meshes_match_the_closed_form(nx, ny, nz, p, permute, seed):
+    """MakeIds box meshes (dawgsMain.cpp:49-143), natural or element-permuted:
+    local and global node counts and the row-degree histogram of the setup
+    equal the closed form (lattice points per axis with multiplicity 1 or 2)."""
+    from dawgs_gb300 import mesh
+    ids = mesh.box_ids(nx, ny, nz, p)
+    if permute:
+        ids = mesh.permute_elements(ids, p, seed=seed)
+    cf = mesh.box_counts(nx, ny, nz, p)
+    g = ogs.ogs_t().Setup(ids.size, ids.copy(), host_only=True)
+    assert (g.N, g.NgatherGlobal) == (cf["local"], cf["global"])
+    assert g.layout_stats()["rows_by_degree"] == cf["rows_by_degree"]
