@@ -41,12 +41,9 @@ sys.path.insert(0, ROOT)
 # and refill the pinned buffer from the CPU: they are capped apart from the
 # kernel steps, which run long enough for several clock samples.
 E2E_STEPS = 30
-# the committed ncu summaries of the default workload, per timed call
-PROFILE_TRAFFIC = {
-    "gs": os.path.join(ROOT, "profiles", "ogs_async_kernel_gs_fp64_add_24x24x24_p7.md"),
-    "gather": os.path.join(ROOT, "profiles", "ogs_async_kernel_gather_trans_fp64_24x24x24_p7.md"),
-    "scatter": os.path.join(ROOT, "profiles", "ogs_async_kernel_scatter_notrans_fp64_24x24x24_p7.md"),
-}
+# the committed ncu summaries: each names the bench workload it captured
+# ("bench_workload: ...") and its DRAM bytes per timed call
+PROFILES = os.path.join(ROOT, "profiles")
 FALLBACK_HBM_GBS = 6800.0
 TYPE_CODE = {"float32": 0, "float64": 1, "int32": 2, "int64": 3}
 OP_CODE = {"add": 0, "mul": 1, "max": 2, "min": 3}
@@ -69,6 +66,11 @@ def parse():
                     help="the timed call: GatherScatter (Sym, Unsigned handle; the headline), or Gather (Trans) / "
                          "Scatter (NoTrans) on a Signed unique handle, as dawgsMain.cpp:174-310 times them")
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--permute", type=int, default=None, metavar="SEED",
+                    help="permute the elements with this seed (the multi-field irregular-access workload "
+                         "uses 32x32x16 p=5 with seed 2024)")
+    ap.add_argument("--many", action="store_true",
+                    help="k separate arrays (ogs_gather_scatter_many) instead of k interleaved components")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
@@ -81,14 +83,21 @@ def parse():
                     help="print the results tables (one JSON line per case) instead of the bench line")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
+    if a.many and a.mode != "gs":
+        ap.error("--many applies to GatherScatter only")
+    if a.many:
+        a.no_e2e = True  # no host-buffer form of the many layout
     return a
 
 
 # ------------------------------------------------------------------ helpers
 class Clocks:
-    """nvidia-smi sampling the GPU every 50 ms while the timed region runs
-    (one streaming process, started before the region and stopped after it;
-    only the samples taken inside the region are kept)."""
+    """nvidia-smi sampling the GPU every 50 ms (one streaming process, started
+    before the region and stopped after it).  `summary()` gives the samples
+    taken inside the region; `mark()` records a narrower timed region inside
+    it, and `summary(marked=True)` reports that region's samples beside those
+    of the whole window (a region shorter than the 50 ms period holds one
+    sample at most)."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -100,6 +109,7 @@ class Clocks:
         self._proc = None
         self._t = None
         self._t0 = self._t1 = None
+        self._m0 = self._m1 = None
 
     def _read(self):
         for line in self._proc.stdout:
@@ -136,15 +146,33 @@ class Clocks:
         inside = [r for t, r in self._all if self._t0 <= t <= self._t1 + 0.06]
         self.rows = inside if inside else [r for _, r in self._all[-1:]]
 
-    def summary(self):
-        if not self.rows:
+    def mark(self, t0, t1):
+        self._m0, self._m1 = t0, t1
+
+    @staticmethod
+    def _stats(rows):
+        if not rows:
             return None
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({n for r in self.rows for n, val in zip(names, r[5:9]) if val.strip() == "Active"})
+        reasons = sorted({n for r in rows for n, val in zip(names, r[5:9]) if val.strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(rows)}
+
+    def summary(self, marked=False):
+        if not marked or self._m0 is None:
+            return self._stats(self.rows)
+        inside = [r for t, r in self._all if self._m0 <= t <= self._m1 + 0.06]
+        out = self._stats(inside) or {"samples": 0}
+        whole = self._stats(self.rows)
+        out["timed_region_ms"] = 1e3 * (self._m1 - self._m0)
+        out["sample_period_ms"] = 50
+        if whole is not None:
+            # every GPU leg of this run (cold and warm kernel loops, e2e, the
+            # baselines): the region above is too short for many 50 ms samples
+            out["whole_run"] = whole
+        return out
 
 
 def hbm_peak():
@@ -156,15 +184,26 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def profiled_traffic(mode="gs"):
-    """dram bytes per launch from the committed ncu summary (same workload)."""
+def profiled_traffic(workload):
+    """(dram bytes per timed call, summary file) from the committed ncu
+    summary of this exact workload, or (None, None)."""
     try:
-        for line in open(PROFILE_TRAFFIC[mode]):
-            if line.strip().startswith("dram_bytes_per_launch:"):
-                return int(line.split(":")[1].strip().replace(",", ""))
+        names = sorted(os.listdir(PROFILES))
     except OSError:
-        pass
-    return None
+        return None, None
+    for fn in names:
+        if not fn.endswith(".md"):
+            continue
+        got_w, got_b = None, None
+        for line in open(os.path.join(PROFILES, fn)):
+            t = line.strip()
+            if t.startswith("bench_workload:"):
+                got_w = t.split(":", 1)[1].strip()
+            elif t.startswith("dram_bytes_per_launch:"):
+                got_b = int(t.split(":")[1].strip().replace(",", ""))
+        if got_w == workload and got_b is not None:
+            return got_b, fn
+    return None, None
 
 
 MODE_NAME = {"gs": "GatherScatter", "gather": "Gather", "scatter": "Scatter"}
@@ -175,8 +214,10 @@ def workload_name(a):
     mode = getattr(a, "mode", "gs")
     op = "" if mode == "scatter" else f" {a.op.capitalize()}"
     handle = "" if mode == "gs" else " (Signed unique handle)"
-    return (f"ogs {MODE_NAME[mode]} {a.dtype}{op} {MODE_TRANS[mode]} k={a.k}{handle}, "
-            f"{a.nx}x{a.ny}x{a.nz} hex box p={a.p}")
+    layout = " separate arrays" if getattr(a, "many", False) else (" interleaved" if a.k > 1 else "")
+    perm = f", elements permuted (seed {a.permute})" if getattr(a, "permute", None) is not None else ""
+    return (f"ogs {MODE_NAME[mode]} {a.dtype}{op} {MODE_TRANS[mode]} k={a.k}{layout}{handle}, "
+            f"{a.nx}x{a.ny}x{a.nz} hex box p={a.p}{perm}")
 
 
 def metric_name(a):
@@ -196,6 +237,8 @@ def alg_bytes(N, nnz, R, k, s, mode="gs", Nglobal=0):
 def make_inputs(a):
     from dawgs_gb300 import mesh
     ids = mesh.box_ids(a.nx, a.ny, a.nz, a.p)
+    if getattr(a, "permute", None) is not None:
+        ids = mesh.permute_elements(ids, a.p, seed=a.permute)
     dt = np.dtype(a.dtype)
     n = a.k * ids.size
     if dt.kind == "f":
@@ -215,7 +258,15 @@ def cpu_reference_run(a, ids, v, warmup, steps):
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
     mode = getattr(a, "mode", "gs")
-    if mode == "gs":
+    if mode == "gs" and getattr(a, "many", False):
+        h = oracle.OracleOgs(ids.copy(), "unsigned")
+        x = v.copy().reshape(a.k, -1)
+
+        def call():
+            for j in range(a.k):
+                h.gather_scatter(x[j], 1, a.op, "sym")
+        reset = lambda: np.copyto(x, v.reshape(a.k, -1))  # noqa: E731
+    elif mode == "gs":
         h = oracle.OracleOgs(ids.copy(), "unsigned")
         x = v.copy()
         call = lambda: h.gather_scatter(x, a.k, a.op, "sym")  # noqa: E731
@@ -538,7 +589,12 @@ def run_ours(a):
     if a.mode == "scatter":
         _lib.check(L.ogs_gather(h, gvd.data_ptr(), pristine.data_ptr(), a.k, tcode, ocode, 2, stream.cuda_stream))
 
+    import ctypes as C
+    many_ptrs = (C.c_void_p * a.k)(*[work.data_ptr() + j * ids.size * s for j in range(a.k)])
+
     def call():
+        if a.many:
+            return L.ogs_gather_scatter_many(h, many_ptrs, a.k, tcode, ocode, 0, stream.cuda_stream)
         if a.mode == "gs":
             return L.ogs_gather_scatter(h, work.data_ptr(), a.k, tcode, ocode, 0, stream.cuda_stream)
         if a.mode == "gather":
@@ -565,20 +621,23 @@ def run_ours(a):
         flush.zero_()
         torch.sum(flush, dim=0, out=sink)
 
+    # clocks are sampled over every GPU leg of the run; the cold timed loop
+    # is marked inside that window
+    clk = Clocks(local).__enter__()
     for _ in range(a.warmup):
         work.copy_(pristine)
         flush_l2()
         step()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
-    with Clocks(local) as clk:
-        barrier()
-        w0 = time.perf_counter()
-        for e0, e1 in evs:
-            work.copy_(pristine)
-            flush_l2()
-            step(e0, e1)
-        barrier()
-        w1 = time.perf_counter()
+    barrier()
+    w0 = time.perf_counter()
+    for e0, e1 in evs:
+        work.copy_(pristine)
+        flush_l2()
+        step(e0, e1)
+    barrier()
+    w1 = time.perf_counter()
+    clk.mark(w0, w1)
     kt = [e0.elapsed_time(e1) * 1e-3 for e0, e1 in evs]
     t_kernel, _, value = aggregate_over_ranks(sum(kt), g.NgatherGlobal * a.steps, dev)
     per_step = t_kernel / a.steps
@@ -603,7 +662,7 @@ def run_ours(a):
     # the reference's device algorithm (OKL gatherScatter, 512-member row
     # blocks) restated in CUDA, timed the same way on the same GPU
     refdev_line = None
-    if not a.no_refdev and rank == 0 and a.mode == "gs":
+    if not a.no_refdev and rank == 0 and a.mode == "gs" and not a.many:
         import refdev
         refdev.build()
         rd = refdev.RefDevOgs(g)
@@ -680,7 +739,11 @@ def run_ours(a):
     if rank == 0 and world == 1 and not a.no_cpu:
         hc, times, cores = cpu_reference_run(a, ids, v, 2, 5)
         x = v.copy()
-        if a.mode == "gs":
+        if a.many:
+            for j in range(a.k):
+                hc.gather_scatter(x[j * ids.size:(j + 1) * ids.size], 1, a.op, "sym")
+            got, host_got = work.cpu().numpy(), None
+        elif a.mode == "gs":
             hc.gather_scatter(x, a.k, a.op, "sym")
             got, host_got = work.cpu().numpy(), (host.numpy() if e2e is not None else None)
         elif a.mode == "gather":
@@ -701,21 +764,24 @@ def run_ours(a):
                "sample": f"5 full {MODE_NAME[a.mode]} calls on this workload after 2 warm-up, OpenMP over "
                          f"{cores} threads; its output is also compared bit for bit with the GPU result"}
 
+    default_workload = (a.mode, a.dtype, a.op, a.k, a.many, a.permute, a.nx, a.ny, a.nz, a.p) == \
+        ("gs", "float64", "add", 1, False, None, 24, 24, 24, 7)
     batched = None
-    if rank == 0 and world == 1 and not a.no_batched and a.mode == "gs":
+    if rank == 0 and world == 1 and not a.no_batched and default_workload:
         batched = run_batched(a, dev, L, stream)
     served = None
-    if rank == 0 and world == 1 and not a.no_served and a.mode == "gs":
+    if rank == 0 and world == 1 and not a.no_served and default_workload:
         served = run_served(a, dev, L, stream)
 
     partitioned = None
-    if (rank == 0 and world == 1 and not a.no_partitioned and a.k == 1 and a.dtype == "float64" and a.op == "add"
-            and a.mode == "gs"):
+    if rank == 0 and world == 1 and not a.no_partitioned and default_workload:
         partitioned = run_partitioned(a, dev, stream, per_step)
 
+    clk.__exit__(None, None, None)
     peak, peak_src = hbm_peak()
     nbytes_alg = alg_bytes(ids.size, g.nnzT, g.NlocalT, a.k, s, a.mode, g.Ngather)
     achieved = nbytes_alg / per_step / 1e9
+    traffic, traffic_src = profiled_traffic(workload_name(a))
     stats = g.layout_stats()
     line = {
         "metric": metric_name(a),
@@ -731,9 +797,14 @@ def run_ours(a):
                    "warp_tiles": stats["nwarp_tiles"], "general_tiles": stats["ngeneral_tiles"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
-                     # the ncu capture covers the default workload only
-                     "traffic": profiled_traffic(a.mode) if (a.dtype, a.op, a.k, a.nx, a.ny, a.nz, a.p) ==
-                     ("float64", "add", 1, 24, 24, 24, 7) else None,
+                     # DRAM bytes one call really moves (ncu, committed summary of this workload),
+                     # and that traffic over this run's time against the same peak: the
+                     # algorithmic frac credits writes that silent stores skip and sectors
+                     # that neighbouring rows share in L2
+                     "traffic": traffic,
+                     "dram_achieved": traffic / per_step / 1e9 if traffic else None,
+                     "dram_frac": traffic / per_step / 1e9 / peak if traffic else None,
+                     "traffic_source": f"profiles/{traffic_src}" if traffic_src else None,
                      "warm": {"ms_per_step": warm_per_step * 1e3, "achieved": nbytes_alg / warm_per_step / 1e9,
                               "frac": nbytes_alg / warm_per_step / 1e9 / peak},
                      "alg_bytes_per_launch": nbytes_alg, "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"
@@ -746,7 +817,7 @@ def run_ours(a):
         "reference_device_equivalent": refdev_line,
         "partitioned": partitioned,
         "gpu_launches": a.steps,
-        "clocks": clk.summary(),
+        "clocks": clk.summary(marked=True),
         "wall_ms_per_step_incl_restore_and_flush": 1e3 * (w1 - w0) / a.steps,
     }
     if rank == 0:

@@ -24,8 +24,6 @@ ogs_status set_error(ogs_status s, const std::string& msg) {
   return s;
 }
 
-namespace {
-
 size_t type_size(int type) { return (type == OGS_DOUBLE || type == OGS_INT64) ? 8 : 4; }
 
 ogs_status check_common(ogs_handle h, int k, int type, int trans, const char* fn) {
@@ -75,6 +73,8 @@ Pattern pattern_for(const ogs_handle_s* h, int mode, int trans) {
   }
   return p;
 }
+
+namespace {
 
 ogs_status launch_maps(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, int type,
                        void* stream, const char* fn) {

@@ -301,4 +301,15 @@ int launch_batch_i64(const BatchEntry* E, const int64_t* starts, int n, int64_t 
 // Thread-local error message (ogs_capi.cpp).
 ogs_status set_error(ogs_status s, const std::string& msg);
 
+// Argument checks and member patterns shared by the entry points (ogs_capi.cpp).
+size_t type_size(int type);
+// handle usable on the current device, k >= 1, known type and transpose; refuses
+// host-only handles and handles made by ogs_gslib_setup
+ogs_status check_common(ogs_handle h, int k, int type, int trans, const char* fn);
+// GatherScatter and Scatter write every member: no local node in two rows
+ogs_status check_writes(ogs_handle h, const char* fn);
+ogs_status check_op(int op, const char* fn);
+// members read and written for (kind, mode, transpose), ogsOperator.cpp:71-79, 214-222, 321-339
+Pattern pattern_for(const ogs_handle_s* h, int mode, int trans);
+
 }  // namespace ogsgb

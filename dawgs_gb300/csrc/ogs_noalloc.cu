@@ -19,7 +19,9 @@
 // without ordering between them) race and corrupt each other's fields.  Each
 // call overwrites the bytes it uses with the caller's field before the
 // kernel reads them, so nothing in the array has to start at zero and what
-// the last call left there is never read.
+// the last call left there is never read.  The cached address of the array
+// belongs to the device's primary context: after a cudaDeviceReset the entry
+// point must not be called again in that process.
 #include <cstddef>
 #include <mutex>
 #include <string>
@@ -42,7 +44,9 @@ std::mutex g_stage_mu;
 void* g_stage_addr[kMaxDevices] = {};
 
 // Device address of the staging array on the current device, looked up once
-// per device (with that device current) and cached.
+// per device (with that device current) and cached for the life of the
+// process.  A cudaDeviceReset destroys the context that address belongs to:
+// after one, this entry point must not be called again in the process.
 ogs_status stage_address(int dev, void** out) {
   std::lock_guard<std::mutex> g(g_stage_mu);
   if (!g_stage_addr[dev]) {
@@ -71,44 +75,38 @@ extern "C" ogs_status ogs_gather_scatter_host_noalloc(ogs_handle h, void* v, int
                                                       void* stream) {
   const char* fn = "ogs_gather_scatter_host_noalloc";
   if (!h) return set_error(OGS_EINVAL, std::string(fn) + ": handle is NULL");
-  if (h->host_only) return set_error(OGS_EINVAL, std::string(fn) + ": handle was set up host-only");
-  if (!h->distinct_cols)
-    return set_error(OGS_EINVAL, std::string(fn) + ": a local node appears in two rows of this operator's map");
   if (k < 1) return set_error(OGS_EINVAL, std::string(fn) + ": k must be >= 1");
   if (type < OGS_FLOAT || type > OGS_INT64) return set_error(OGS_EINVAL, std::string(fn) + ": unknown type");
-  if (op < OGS_ADD || op > OGS_MIN) return set_error(OGS_EINVAL, std::string(fn) + ": unknown op");
-  if (trans < OGS_SYM || trans > OGS_TRANS) return set_error(OGS_EINVAL, std::string(fn) + ": unknown transpose");
+  // The field must fit the array: N*k*sizeof(T) <= kNoAllocStageBytes, tested
+  // by division so that no product can wrap around.
+  const size_t ts = type_size(type);
+  if (h->N > 0 && static_cast<size_t>(k) > kNoAllocStageBytes / ts / static_cast<size_t>(h->N))
+    return set_error(OGS_ERANGE, std::string(fn) + ": the field (" + std::to_string(h->N) + " nodes x k=" +
+                                     std::to_string(k) + " x " + std::to_string(ts) + " bytes) is larger than the " +
+                                     std::to_string(kNoAllocStageBytes) +
+                                     "-byte staging array; use ogs_gather_scatter_host");
+  // the same refusals as ogs_gather_scatter_host (host-only and gslib handles,
+  // a local node in two rows, unknown op or transpose, another device)
+  ogs_status s = check_common(h, k, type, trans, fn);
+  if (s == OGS_OK) s = check_writes(h, fn);
+  if (s == OGS_OK) s = check_op(op, fn);
+  if (s != OGS_OK) return s;
   if (h->N == 0) return OGS_OK;
   if (!v) return set_error(OGS_EINVAL, std::string(fn) + ": v is NULL");
-  const size_t ts = (type == OGS_DOUBLE || type == OGS_INT64) ? 8 : 4;
   const size_t bytes = static_cast<size_t>(h->N) * static_cast<size_t>(k) * ts;
-  if (bytes > kNoAllocStageBytes)
-    return set_error(OGS_ERANGE, std::string(fn) + ": the field takes " + std::to_string(bytes) +
-                                     " bytes, more than the " + std::to_string(kNoAllocStageBytes) +
-                                     "-byte staging array; use ogs_gather_scatter_host");
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-  if (dev != h->device)
-    return set_error(OGS_EINVAL, std::string(fn) + ": handle lives on device " + std::to_string(h->device) +
-                                     ", current device is " + std::to_string(dev));
+  const int dev = h->device;
   if (dev < 0 || dev >= kMaxDevices) return set_error(OGS_ERANGE, std::string(fn) + ": device index too large");
   void* stage = nullptr;
-  ogs_status s = stage_address(dev, &stage);
-  if (s != OGS_OK) return s;
+  if ((s = stage_address(dev, &stage)) != OGS_OK) return s;
 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
   if ((e = cudaMemcpyAsync(stage, v, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) return cuda_fail(e, "copy in");
-  // Members read and written, as for ogs_gather_scatter (ogsOperator.cpp:321-339).
-  Pattern pat{0, 0, 0};
-  if (h->kind == OGS_SIGNED) {
-    if (trans == OGS_TRANS) pat = Pattern{0, 1, 1};
-    else if (trans == OGS_NOTRANS) pat = Pattern{1, 0, 0};
-  }
   FieldArgs f{};
   f.v = stage;
   f.K = k;
   int le = 0;
+  const Pattern pat = pattern_for(h, kModeGS, trans);
   switch (type) {
     case OGS_FLOAT: le = launch_f32(h->dmaps, f, kModeGS, op, pat, stream); break;
     case OGS_DOUBLE: le = launch_f64(h->dmaps, f, kModeGS, op, pat, stream); break;

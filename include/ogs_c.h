@@ -149,7 +149,11 @@ ogs_status ogs_scatter_host(ogs_handle h, void *v, const void *gv, int k, int ty
  * that first call before any stream capture begins.  All calls share the one
  * array: calls that overlap on the GPU race.  Nothing in it needs to start
  * at zero: each call copies its whole field in before the kernel reads it.
- * Same results as ogs_gather_scatter_host, bit for bit. */
+ * The array's address is that of the device's primary context: after a
+ * cudaDeviceReset, do not call this entry point again in the process.
+ * Same refusals and the same results as ogs_gather_scatter_host, bit for bit;
+ * the size is checked first, so an oversized field gets OGS_ERANGE whatever
+ * the handle. */
 ogs_status ogs_gather_scatter_host_noalloc(ogs_handle h, void *v, int k, int type, int op, int trans,
                                            void *stream);
 

@@ -18,7 +18,19 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libogs_oracle.so")
 GSREF_SO = os.path.join(HERE, "_ref", "libgsref.so")
-REFERENCE_GSLIB = "/root/reference/3rdParty/gslib/src"
+
+
+def gslib_src() -> str | None:
+    """The reference's vendored gslib sources: $GSLIB_SRC, else the default of
+    the build recipe (oracle/Makefile); None when that directory is absent."""
+    src = os.environ.get("GSLIB_SRC")
+    if not src:
+        try:
+            src = subprocess.run(["make", "-s", "-C", HERE, "print-gslib-src"], check=True,
+                                 capture_output=True, text=True).stdout.strip()
+        except (OSError, subprocess.CalledProcessError):
+            return None
+    return src if src and os.path.isdir(src) else None
 
 TYPES = {"float32": 0, "float64": 1, "int32": 2, "int64": 3}
 NP_OF = {0: np.float32, 1: np.float64, 2: np.int32, 3: np.int64}
@@ -30,10 +42,11 @@ KINDS = {"unsigned": 0, "signed": 1}
 def build(ref: bool | None = None) -> None:
     """Compile the oracle (and gslib when the reference tree is present)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if ref is None:
-        ref = os.path.isdir(REFERENCE_GSLIB)
-    if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    src = gslib_src() if ref is not False else None
+    if ref and src is None:
+        raise FileNotFoundError("gslib sources not found: set GSLIB_SRC to the reference's 3rdParty/gslib/src")
+    if src is not None:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"GSLIB_SRC={src}"], check=True)
 
 
 _lib = None

@@ -78,6 +78,25 @@ def test_host_only_handle_rejects_ops(built_lib):
     assert built_lib.ogs_gather_scatter(None, v.ctypes.data, 1, 1, 0, 0, None) == _lib.OGS_EINVAL
 
 
+def test_noalloc_size_check_cannot_wrap(built_lib):
+    """The fixed staging array's size check is done by division: k near
+    INT_MAX with 8-byte values (a product past 2^64 for large N) is refused
+    with OGS_ERANGE before anything is copied, whatever the handle."""
+    ids = np.arange(1, 1001, dtype=np.int64)
+    st, h = _setup(ids)
+    assert st == _lib.OGS_OK
+    v = np.zeros(8)
+    try:
+        for k in (2 ** 31 - 1, 2 ** 30, 4195):  # 1000 nodes x 8 B x 4195 > 32 MiB
+            assert built_lib.ogs_gather_scatter_host_noalloc(h, v.ctypes.data, k, 1, 0, 0, None) == _lib.OGS_ERANGE
+            assert b"staging array" in built_lib.ogs_last_error_string()
+        # a field that fits goes on to the usual refusals (a host-only handle)
+        assert built_lib.ogs_gather_scatter_host_noalloc(h, v.ctypes.data, 1, 1, 0, 0, None) == _lib.OGS_EINVAL
+        assert b"host-only" in built_lib.ogs_last_error_string()
+    finally:
+        built_lib.ogs_free(h)
+
+
 def test_python_mirror_raises(built_lib):
     ids = np.array([1, 2, 1, 3], np.int64)
     with pytest.raises(_lib.OgsError) as e:
