@@ -36,6 +36,9 @@ SIGNATURES = {
     "ogs_gather": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _vp]),
     "ogs_scatter": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp]),
     "ogs_gather_scatter_host": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),
+    "ogs_reserve_host": (_i, [_vp, _i, _i]),
+    "ogs_debug_fail_alloc": (_i, [_i64]),
+    "ogs_debug_allocations": (_i, [_vp, _vp, _vp, _vp]),
     "ogs_gather_host": (_i, [_vp, _vp, _vp, _i, _i, _i, _i, _vp]),
     "ogs_scatter_host": (_i, [_vp, _vp, _vp, _i, _i, _i, _vp]),
     "ogs_gather_scatter_host_noalloc": (_i, [_vp, _vp, _i, _i, _i, _i, _vp]),
@@ -58,6 +61,10 @@ SIGNATURES = {
     "ogs_server_submit": (_i, [_vp, _vp, C.c_double, _vp]),
     "ogs_server_clock": (C.c_double, []),
     "ogs_server_wait": (_i, [_vp, _i64]),
+    "ogs_server_wait_for": (_i, [_vp, _i64, C.c_double]),
+    "ogs_server_cancel": (_i, [_vp, _i64, _vp]),
+    "ogs_server_state": (_i, [_vp, _i64, _vp]),
+    "ogs_server_times": (_i, [_vp, _i64, _i64, _vp, _vp, _vp]),
     "ogs_server_drain": (_i, [_vp]),
     "ogs_server_latencies": (_i, [_vp, _i64, _i64, _vp, _vp]),
     "ogs_server_counters": (_i, [_vp, _vp, _vp]),

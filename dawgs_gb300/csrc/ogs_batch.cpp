@@ -32,7 +32,9 @@ namespace {
 
 ogs_status cuda_err(cudaError_t e, const char* fn, const char* what) {
   if (e == cudaSuccess) return OGS_OK;
-  return set_error(OGS_EDEVICE, std::string(fn) + ": " + what + ": " + cudaGetErrorString(e));
+  cudaGetLastError();
+  return set_error(e == cudaErrorMemoryAllocation ? OGS_ENOMEM : OGS_EDEVICE,
+                   std::string(fn) + ": " + what + ": " + cudaGetErrorString(e));
 }
 
 // Members read and written per transpose, as pattern_for in ogs_capi.cpp.
@@ -140,8 +142,8 @@ ogs_status ogs_batch_create(ogs_batch* out, int type, const ogs_batch_entry* ent
     b->starts.push_back(b->starts.back() + static_cast<int64_t>(e.h->dmaps.nwtiles) * e.k);
     if (e.h->dmaps.ngtiles > 0) b->general.push_back(i);
   }
-  if ((s = cuda_err(cudaMalloc(&b->d_entries, sizeof(BatchEntry) * n), fn, "malloc")) != OGS_OK ||
-      (s = cuda_err(cudaMalloc(&b->d_starts, sizeof(int64_t) * (n + 1)), fn, "malloc")) != OGS_OK ||
+  if ((s = cuda_err(dev_malloc(&b->d_entries, sizeof(BatchEntry) * n), fn, "malloc")) != OGS_OK ||
+      (s = cuda_err(dev_malloc(&b->d_starts, sizeof(int64_t) * (n + 1)), fn, "malloc")) != OGS_OK ||
       (s = cuda_err(cudaMemcpy(b->d_entries, b->host_entries.data(), sizeof(BatchEntry) * n,
                                cudaMemcpyHostToDevice), fn, "copy")) != OGS_OK ||
       (s = cuda_err(cudaMemcpy(b->d_starts, b->starts.data(), sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice),
@@ -157,8 +159,8 @@ ogs_status ogs_batch_free(ogs_batch b) {
   if (!b) return OGS_OK;
   drop_graph(b);
   if (b->capture) cudaStreamDestroy(b->capture);
-  if (b->d_entries) cudaFree(b->d_entries);
-  if (b->d_starts) cudaFree(b->d_starts);
+  if (b->d_entries) dev_free(b->d_entries);
+  if (b->d_starts) dev_free(b->d_starts);
   delete b;
   return OGS_OK;
 }

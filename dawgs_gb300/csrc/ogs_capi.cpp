@@ -98,10 +98,10 @@ ogs_status launch(const ogs_handle_s* h, const FieldArgs& f, int mode, int op, P
 
 ogs_status ensure_stage(ogs_handle_s* h, size_t bytes, const char* fn) {
   if (bytes <= h->stage_bytes) return OGS_OK;
-  if (h->stage) cudaFree(h->stage);
+  if (h->stage) dev_free(h->stage);
   h->stage = nullptr;
   h->stage_bytes = 0;
-  cudaError_t e = cudaMalloc(&h->stage, bytes);
+  cudaError_t e = dev_malloc(&h->stage, bytes);
   if (e != cudaSuccess) {
     cudaGetLastError();
     h->stage = nullptr;
@@ -367,6 +367,7 @@ ogs_status ogs_gather_scatter_host(ogs_handle h, void* v, int k, int type, int o
   if (s != OGS_OK) return s;
   if (h->N == 0) return OGS_OK;
   if (!v) return set_error(OGS_EINVAL, "ogs_gather_scatter_host: v is NULL");
+  std::lock_guard<std::mutex> host_lock(h->host_mu);
   const size_t node_bytes = static_cast<size_t>(k) * type_size(type);
   const size_t bytes = static_cast<size_t>(h->N) * node_bytes;
   if ((s = ensure_stage(h, bytes, fn)) != OGS_OK) return s;
@@ -519,6 +520,7 @@ ogs_status ogs_gather_host(ogs_handle h, void* gv, const void* v, int k, int typ
   if (!h->gather_defined) return set_error(OGS_EUNDEFINED, "Gather operation not well-defined.");
   if (h->N == 0 || h->NlocalT == 0) return OGS_OK;
   if (!gv || !v) return set_error(OGS_EINVAL, "ogs_gather_host: NULL buffer");
+  std::lock_guard<std::mutex> host_lock(h->host_mu);
   const size_t ts = type_size(type);
   const size_t vb = static_cast<size_t>(h->N) * k * ts;
   const size_t voff = (vb + 255) / 256 * 256;
@@ -553,6 +555,7 @@ ogs_status ogs_scatter_host(ogs_handle h, void* v, const void* gv, int k, int ty
   if (!h->gather_defined) return set_error(OGS_EUNDEFINED, "Gather operation not well-defined.");
   if (h->N == 0 || h->NlocalT == 0) return OGS_OK;
   if (!gv || !v) return set_error(OGS_EINVAL, "ogs_scatter_host: NULL buffer");
+  std::lock_guard<std::mutex> host_lock(h->host_mu);
   const size_t ts = type_size(type);
   const size_t vb = static_cast<size_t>(h->N) * k * ts;
   const size_t voff = (vb + 255) / 256 * 256;
@@ -589,6 +592,22 @@ ogs_status ogs_scatter_host(ogs_handle h, void* v, const void* gv, int k, int ty
   if ((s = cuda_status(cudaMemcpyAsync(v, base, vb, cudaMemcpyDeviceToHost, st), fn, "copy out")) != OGS_OK)
     return s;
   return cuda_status(cudaStreamSynchronize(st), fn, "synchronize");
+}
+
+ogs_status ogs_reserve_host(ogs_handle h, int k, int type) {
+  const char* fn = "ogs_reserve_host";
+  ogs_status s = check_common(h, k, type, OGS_SYM, fn);
+  if (s != OGS_OK) return s;
+  if (h->N == 0) return OGS_OK;
+  // the largest staging any _host call takes for this k and type: the field,
+  // 256-byte aligned, then the gathered vector (Gather / Scatter)
+  const size_t nb = static_cast<size_t>(k) * type_size(type);
+  const size_t voff = (static_cast<size_t>(h->N) * nb + 255) / 256 * 256;
+  const size_t bytes = voff + static_cast<size_t>(h->NlocalT) * nb;
+  std::lock_guard<std::mutex> host_lock(h->host_mu);
+  if ((s = ensure_stage(h, bytes, fn)) != OGS_OK) return s;
+  if (h->lay.phases.size() >= 2) return ensure_pipeline(h, fn);
+  return OGS_OK;
 }
 
 ogs_status ogs_get_counts(ogs_handle h, ogs_counts* out) {

@@ -344,13 +344,13 @@ __global__ void k_wemask(const Tile* __restrict__ wt, int64_t nw, BucketPtrs B, 
 struct Scratch {
   std::vector<void*> bufs;
   ~Scratch() {
-    for (void* p : bufs) cudaFree(p);
+    for (void* p : bufs) dev_free(p);
   }
   template <typename T>
   cudaError_t get(T** p, int64_t count) {
     void* q = nullptr;
     const size_t bytes = static_cast<size_t>(count > 0 ? count : 1) * sizeof(T);
-    const cudaError_t e = cudaMalloc(&q, bytes);
+    const cudaError_t e = dev_malloc(&q, bytes);
     if (e == cudaSuccess) bufs.push_back(q);
     *p = static_cast<T*>(q);
     return e;
@@ -540,9 +540,9 @@ ogs_status build_device_layout(ogs_handle_s* h, const int32_t* rsT, const int32_
   int dev = 0;
   if ((e = cudaGetDevice(&dev))) return fail(e, "device");
   char* base = nullptr;
-  if ((e = cudaMalloc(reinterpret_cast<void**>(&base), total))) return fail(e, "arena");
+  if ((e = dev_malloc(reinterpret_cast<void**>(&base), total))) return fail(e, "arena");
   auto release = [&](cudaError_t err, const char* what) {
-    cudaFree(base);
+    dev_free(base);
     return fail(err, what);
   };
   if ((e = cudaMemsetAsync(base, 0, total, st))) return release(e, "arena");

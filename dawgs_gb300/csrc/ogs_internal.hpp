@@ -6,8 +6,11 @@
 
 #include <atomic>
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <vector>
+
+#include <cuda_runtime_api.h>
 
 #include "ogs_c.h"
 
@@ -250,6 +253,7 @@ struct ogs_handle_s {
   size_t arena_bytes = 0;
   ogsgb::DevMaps dmaps{};
 
+  std::mutex host_mu;     // serialises the _host entry points (they share `stage`)
   void* stage = nullptr;  // device staging for the _host entry points
   size_t stage_bytes = 0;
   void* copy_in = nullptr;   // cudaStream_t: host->device chunks of the host pipeline
@@ -297,6 +301,22 @@ int launch_batch_f32(const BatchEntry* E, const int64_t* starts, int n, int64_t 
 int launch_batch_f64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream);
 int launch_batch_i32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream);
 int launch_batch_i64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream);
+
+// Device and page-locked host allocations (ogs_alloc.cpp): counted, and made
+// to fail on demand by ogs_debug_fail_alloc.  Every allocation of the library
+// goes through these.
+cudaError_t dev_malloc_raw(void** p, size_t bytes);
+void dev_free(void* p);
+cudaError_t host_malloc_raw(void** p, size_t bytes);
+void host_free(void* p);
+template <typename T>
+inline cudaError_t dev_malloc(T** p, size_t bytes) {
+  return dev_malloc_raw(reinterpret_cast<void**>(p), bytes);
+}
+template <typename T>
+inline cudaError_t host_malloc(T** p, size_t bytes) {
+  return host_malloc_raw(reinterpret_cast<void**>(p), bytes);
+}
 
 // Thread-local error message (ogs_capi.cpp).
 ogs_status set_error(ogs_status s, const std::string& msg);

@@ -3,16 +3,26 @@
 //
 // A request names a resident mesh and carries a host field (k interleaved
 // components per node) that is gather-scattered in place.  One worker thread
-// runs the service loop:
-//   admit   -- FIFO: a pending request is admitted when a field buffer of its
-//              size fits in the budget pool and an in-flight slot is free;
-//   launch  -- everything admitted since the last turn is copied in on the
-//              copy-in stream and run as one batched launch per value type
-//              (ogs_batch.cuh) on the next of two compute streams, so a batch
-//              that arrives while another runs overlaps with it on the GPU;
+// runs the service loop and never blocks on the GPU:
 //   retire  -- each request's copy-out records an event; the worker polls the
-//              oldest outstanding events, stamps completions and returns the
-//              buffers to the pool.
+//              oldest outstanding events of each lane, stamps completions and
+//              returns the buffers to the pool;
+//   admit   -- pending requests are scanned in arrival order, up to
+//              kAdmitWindow of them: each one whose field buffer fits in the
+//              budget pool (and while in-flight slots remain) is admitted, so
+//              one large request cannot hold back the small ones behind it.
+//              A request passed over kMaxPassOvers times stops the scan at
+//              itself until it fits (no starvation);
+//   launch  -- admitted requests go to one of two lanes by size (small fields
+//              and large fields), each with its own copy-in, compute and
+//              copy-out streams: a small request never waits behind a large
+//              request's copies.  Everything admitted to a lane since its last
+//              turn is copied in and run as one batched launch per value type
+//              (ogs_batch.cuh).  A launch needs a table slot whose previous
+//              launch is over; when none is free the lane waits for the next
+//              turn instead of blocking the worker.
+// Requests arriving while others are on the GPU are admitted and launched on
+// the next turn, so their copies and kernels overlap the earlier ones'.
 // Latency is completion minus arrival (the submit time, or the arrival time the
 // caller passes).  Every result equals the request's ogs_gather_scatter_host
 // alone, bit for bit: batching changes where the rows run, not their fold.
@@ -42,7 +52,16 @@ double now_s() {
   return duration<double>(steady_clock::now().time_since_epoch()).count();
 }
 
-size_t tsize(int type) { return (type == OGS_DOUBLE || type == OGS_INT64) ? 8 : 4; }
+// Pending requests looked at per admission pass, and how often one may be
+// passed over by later requests before the scan stops at it.
+constexpr int kAdmitWindow = 64;
+constexpr int kMaxPassOvers = 16;
+// Fields up to this size go to the small lane.
+constexpr size_t kSmallBytes = size_t(4) << 20;
+// Launch tables per server (shared by both lanes).
+constexpr int kTableSlots = 64;
+
+enum ReqState : int { kPending = 0, kInFlight = 1, kDone = 2, kCancelled = 3 };
 
 // First-fit allocator over one device arena, 256-byte granules.
 class Pool {
@@ -90,8 +109,9 @@ struct Req {
   ogs_server_request r;
   size_t bytes = 0;
   size_t off = 0;
-  double t_arrival = 0, t_done = 0;
-  std::atomic<int> state{0};  // 0 pending, 1 in flight, 2 done
+  double t_arrival = 0, t_launch = -1, t_done = -1;
+  int passed_over = 0;
+  std::atomic<int> state{kPending};
   cudaEvent_t copied_out = nullptr;
 };
 
@@ -105,6 +125,14 @@ struct TableSlot {
   bool used = false;
 };
 
+// Streams and queues of one size class.
+struct Lane {
+  cudaStream_t in = nullptr, compute = nullptr, out = nullptr;
+  cudaEvent_t copied = nullptr;  // all of a turn's copies in are done
+  std::vector<Req*> ready;       // admitted, not yet launched (worker only)
+  std::deque<Req*> outstanding;  // launched, in copy-out order (worker only)
+};
+
 }  // namespace
 }  // namespace ogsgb
 
@@ -115,9 +143,10 @@ struct ogs_server_s {
   int device = 0;
   std::vector<ogs_handle> meshes;
   char* pool_base = nullptr;
+  char* d_tables = nullptr;  // every slot's device tables, one allocation
+  char* h_tables = nullptr;  // and their pinned staging
   Pool pool;
-  cudaStream_t copy_in = nullptr, copy_out = nullptr, compute[2] = {nullptr, nullptr};
-  int next_compute = 0;
+  Lane lanes[2];  // [0] small fields, [1] large fields
   std::vector<TableSlot> slots;
   size_t next_slot = 0;
 
@@ -125,8 +154,7 @@ struct ogs_server_s {
   std::condition_variable cv;
   std::deque<Req*> pending;
   std::vector<std::unique_ptr<Req>> all;  // by id
-  std::deque<Req*> outstanding;          // launched, in copy-out order (worker only)
-  std::vector<cudaEvent_t> spare_events; // recycled completion events (worker only)
+  std::vector<cudaEvent_t> spare_events;  // recycled completion events (worker only)
   std::atomic<int64_t> inflight{0}, completed{0}, submitted{0};
   std::atomic<int64_t> launches{0}, batched_requests{0};
   std::thread worker;
@@ -161,11 +189,32 @@ int general_launch(int type, const ogs_handle_s* h, void* v, int k, int op, cons
   }
 }
 
-// Launch one group of admitted requests of one value type; returns a CUDA error.
-int launch_group(ogs_server_s* s, const std::vector<Req*>& grp, int type, cudaEvent_t copied) {
-  TableSlot& slot = s->slots[s->next_slot];
-  s->next_slot = (s->next_slot + 1) % s->slots.size();
-  if (slot.used) cudaEventSynchronize(slot.done);  // its previous launch must be over
+// Free table slots (their previous launch is over), without waiting; at most
+// `want` of them.  A failed query is recorded as the server's error.
+std::vector<TableSlot*> free_slots(ogs_server_s* s, int want) {
+  std::vector<TableSlot*> got;
+  const size_t n = s->slots.size();
+  for (size_t j = 0; j < n && static_cast<int>(got.size()) < want; ++j) {
+    TableSlot& t = s->slots[(s->next_slot + j) % n];
+    if (t.used) {
+      const cudaError_t e = cudaEventQuery(t.done);
+      if (e == cudaErrorNotReady) continue;
+      if (e != cudaSuccess) {
+        std::lock_guard<std::mutex> g(s->mu);
+        if (s->error.empty()) s->error = cudaGetErrorString(e);
+        continue;
+      }
+      t.used = false;
+    }
+    got.push_back(&t);
+  }
+  if (!got.empty()) s->next_slot = (static_cast<size_t>(got.back() - s->slots.data()) + 1) % n;
+  return got;
+}
+
+// Launch one group of a lane's requests of one value type on the lane's
+// compute stream, after the lane's copies in; queue their copies out.
+int launch_group(ogs_server_s* s, Lane& lane, TableSlot& slot, const std::vector<Req*>& grp, int type) {
   const int n = static_cast<int>(grp.size());
   slot.h_starts[0] = 0;
   for (int i = 0; i < n; ++i) {
@@ -178,18 +227,17 @@ int launch_group(ogs_server_s* s, const std::vector<Req*>& grp, int type, cudaEv
     e.v = s->pool_base + q->off;
     e.K = q->r.k;
     e.op = q->r.op;
-    if (h->kind == OGS_SIGNED) {
-      if (q->r.trans == OGS_TRANS) e.scatter_n = e.limit_n = 1;
-      else if (q->r.trans == OGS_NOTRANS) e.gather_n = 1;
-    }
+    const Pattern p = pattern_for(h, kModeGS, q->r.trans);
+    e.gather_n = p.gather_n;
+    e.scatter_n = p.scatter_n;
+    e.limit_n = p.limit_n;
     e.use_mask = (e.gather_n || e.scatter_n) && h->kind == OGS_SIGNED;
     slot.h_starts[i + 1] = slot.h_starts[i] + static_cast<int64_t>(h->dmaps.nwtiles) * q->r.k;
   }
-  cudaStream_t st = s->compute[s->next_compute];
-  s->next_compute ^= 1;
+  cudaStream_t st = lane.compute;
   int e = cudaMemcpyAsync(slot.d_entries, slot.h_entries, sizeof(BatchEntry) * n, cudaMemcpyHostToDevice, st);
   if (!e) e = cudaMemcpyAsync(slot.d_starts, slot.h_starts, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st);
-  if (!e) e = cudaStreamWaitEvent(st, copied, 0);
+  if (!e) e = cudaStreamWaitEvent(st, lane.copied, 0);
   if (!e) e = batch_launch(type, slot.d_entries, slot.d_starts, n, slot.h_starts[n], st);
   for (int i = 0; !e && i < n; ++i) {
     const Req* q = grp[i];
@@ -201,22 +249,22 @@ int launch_group(ogs_server_s* s, const std::vector<Req*>& grp, int type, cudaEv
   }
   if (!e) e = cudaEventRecord(slot.done, st);
   slot.used = true;
-  if (!e) e = cudaStreamWaitEvent(s->copy_out, slot.done, 0);
+  const double t = now_s();
+  if (!e) e = cudaStreamWaitEvent(lane.out, slot.done, 0);
   for (int i = 0; !e && i < n; ++i) {
     Req* q = grp[i];
-    e = cudaMemcpyAsync(q->r.host, s->pool_base + q->off, q->bytes, cudaMemcpyDeviceToHost, s->copy_out);
-    if (!e) {
-      if (s->spare_events.empty()) {
-        cudaEvent_t ev = nullptr;
-        e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
-        if (!e) s->spare_events.push_back(ev);
-      }
+    q->t_launch = t;
+    e = cudaMemcpyAsync(q->r.host, s->pool_base + q->off, q->bytes, cudaMemcpyDeviceToHost, lane.out);
+    if (!e && s->spare_events.empty()) {
+      cudaEvent_t ev = nullptr;
+      e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+      if (!e) s->spare_events.push_back(ev);
     }
     if (!e) {
       q->copied_out = s->spare_events.back();
       s->spare_events.pop_back();
-      e = cudaEventRecord(q->copied_out, s->copy_out);
-      s->outstanding.push_back(q);
+      e = cudaEventRecord(q->copied_out, lane.out);
+      lane.outstanding.push_back(q);
     }
   }
   s->launches.fetch_add(1);
@@ -224,15 +272,37 @@ int launch_group(ogs_server_s* s, const std::vector<Req*>& grp, int type, cudaEv
   return e;
 }
 
-// Completions arrive in copy-out order: poll from the oldest.
-void retire(ogs_server_s* s) {
+// Launch what a lane has ready, when enough table slots are free.
+int launch_lane(ogs_server_s* s, Lane& lane) {
+  if (lane.ready.empty()) return 0;
+  std::vector<Req*> grp[4];
+  int groups = 0;
+  for (Req* q : lane.ready) {
+    if (grp[q->r.type].empty()) groups++;
+    grp[q->r.type].push_back(q);
+  }
+  std::vector<TableSlot*> slots = free_slots(s, groups);
+  if (static_cast<int>(slots.size()) < groups) return 0;  // next turn
+  int e = 0;
+  for (Req* q : lane.ready)
+    if (!e) e = cudaMemcpyAsync(s->pool_base + q->off, q->r.host, q->bytes, cudaMemcpyHostToDevice, lane.in);
+  if (!e) e = cudaEventRecord(lane.copied, lane.in);
+  int j = 0;
+  for (int type = OGS_FLOAT; !e && type <= OGS_INT64; ++type)
+    if (!grp[type].empty()) e = launch_group(s, lane, *slots[j++], grp[type], type);
+  lane.ready.clear();
+  return e;
+}
+
+// Completions arrive in copy-out order within a lane: poll from the oldest.
+void retire(ogs_server_s* s, Lane& lane) {
   int n = 0;
-  while (!s->outstanding.empty()) {
-    Req* q = s->outstanding.front();
+  while (!lane.outstanding.empty()) {
+    Req* q = lane.outstanding.front();
     const cudaError_t e = cudaEventQuery(q->copied_out);
     if (e == cudaErrorNotReady) break;
     const double t = now_s();
-    s->outstanding.pop_front();
+    lane.outstanding.pop_front();
     s->spare_events.push_back(q->copied_out);
     q->copied_out = nullptr;
     {
@@ -240,7 +310,7 @@ void retire(ogs_server_s* s) {
       if (e != cudaSuccess && s->error.empty()) s->error = cudaGetErrorString(e);
       s->pool.release(q->off, q->bytes);
       q->t_done = t;
-      q->state.store(2);
+      q->state.store(kDone);
       s->inflight.fetch_sub(1);
     }
     s->completed.fetch_add(1);
@@ -249,66 +319,90 @@ void retire(ogs_server_s* s) {
   if (n) s->cv.notify_all();
 }
 
+// Admission pass (s->mu held): requests that fit, in arrival order, within
+// the window.  Every admission counts as a pass-over for each earlier request
+// of the pass that did not fit; one passed over kMaxPassOvers times stops the
+// scan at itself, so it is the next to be admitted once memory frees up.
+void admit(ogs_server_s* s) {
+  int looked = 0;
+  std::vector<Req*> blocked;
+  for (auto it = s->pending.begin(); it != s->pending.end() && looked < kAdmitWindow;) {
+    if (s->inflight.load() >= s->cfg.max_inflight) break;
+    Req* q = *it;
+    looked++;
+    Lane& lane = s->lanes[q->bytes <= kSmallBytes ? 0 : 1];
+    if (static_cast<int>(lane.ready.size()) < s->cfg.max_batch && s->pool.alloc(q->bytes, &q->off)) {
+      it = s->pending.erase(it);
+      q->state.store(kInFlight);
+      s->inflight.fetch_add(1);
+      lane.ready.push_back(q);
+      for (Req* b : blocked) b->passed_over++;
+      continue;
+    }
+    if (q->passed_over >= kMaxPassOvers) break;  // nothing later may pass it any more
+    blocked.push_back(q);
+    ++it;
+  }
+}
+
 void worker_loop(ogs_server_s* s) {
   cudaSetDevice(s->device);
-  cudaEvent_t copied = nullptr;
-  cudaEventCreateWithFlags(&copied, cudaEventDisableTiming);
-  std::vector<Req*> admitted;
   while (true) {
-    retire(s);
+    for (Lane& l : s->lanes) retire(s, l);
+    bool idle;
     {
       std::unique_lock<std::mutex> lk(s->mu);
-      if (s->pending.empty() && s->stop.load() && s->inflight.load() == 0) break;
-      // admission: FIFO against the budget and the in-flight slots
-      while (!s->pending.empty() && s->inflight.load() < s->cfg.max_inflight &&
-             static_cast<int>(admitted.size()) < s->cfg.max_batch) {
-        Req* q = s->pending.front();
-        if (!s->pool.alloc(q->bytes, &q->off)) break;
-        s->pending.pop_front();
-        q->state.store(1);
-        s->inflight.fetch_add(1);
-        admitted.push_back(q);
-      }
-      if (admitted.empty()) {
+      const bool nothing_out = s->lanes[0].outstanding.empty() && s->lanes[1].outstanding.empty();
+      const bool nothing_ready = s->lanes[0].ready.empty() && s->lanes[1].ready.empty();
+      if (s->pending.empty() && nothing_ready && s->stop.load() && s->inflight.load() == 0) break;
+      admit(s);
+      idle = s->lanes[0].ready.empty() && s->lanes[1].ready.empty();
+      if (idle) {
         // nothing to launch: wait for a submission, or come back soon to
         // retire what is in flight (which may free budget for the pending)
-        s->cv.wait_for(lk, std::chrono::microseconds(s->outstanding.empty() ? 500 : 20));
+        s->cv.wait_for(lk, std::chrono::microseconds(nothing_out ? 500 : 20));
         continue;
       }
     }
-    int e = 0;
-    for (Req* q : admitted)
-      if (!e) e = cudaMemcpyAsync(s->pool_base + q->off, q->r.host, q->bytes, cudaMemcpyHostToDevice, s->copy_in);
-    if (!e) e = cudaEventRecord(copied, s->copy_in);
-    for (int type = OGS_FLOAT; !e && type <= OGS_INT64; ++type) {
-      std::vector<Req*> grp;
-      for (Req* q : admitted)
-        if (q->r.type == type) grp.push_back(q);
-      if (!grp.empty()) e = launch_group(s, grp, type, copied);
+    for (Lane& l : s->lanes) {
+      const int e = launch_lane(s, l);
+      if (e) {
+        std::lock_guard<std::mutex> g(s->mu);
+        if (s->error.empty()) s->error = cudaGetErrorString(static_cast<cudaError_t>(e));
+      }
     }
-    if (e) {
-      std::lock_guard<std::mutex> g(s->mu);
-      s->error = cudaGetErrorString(static_cast<cudaError_t>(e));
+    {
+      // a lane left waiting for a table slot: let launches finish
+      std::unique_lock<std::mutex> lk(s->mu);
+      if (!s->lanes[0].ready.empty() || !s->lanes[1].ready.empty())
+        s->cv.wait_for(lk, std::chrono::microseconds(10));
     }
-    admitted.clear();
   }
-  cudaEventDestroy(copied);
 }
 
 void destroy(ogs_server_s* s) {
   for (cudaEvent_t ev : s->spare_events) cudaEventDestroy(ev);
-  for (TableSlot& t : s->slots) {
-    if (t.d_entries) cudaFree(t.d_entries);
-    if (t.d_starts) cudaFree(t.d_starts);
-    if (t.h_entries) cudaFreeHost(t.h_entries);
-    if (t.h_starts) cudaFreeHost(t.h_starts);
+  for (auto& q : s->all)
+    if (q->copied_out) cudaEventDestroy(q->copied_out);
+  for (TableSlot& t : s->slots)
     if (t.done) cudaEventDestroy(t.done);
+  dev_free(s->d_tables);
+  host_free(s->h_tables);
+  for (Lane& l : s->lanes) {
+    for (cudaStream_t st : {l.in, l.compute, l.out})
+      if (st) cudaStreamDestroy(st);
+    if (l.copied) cudaEventDestroy(l.copied);
   }
-  for (cudaStream_t st : {s->copy_in, s->copy_out, s->compute[0], s->compute[1]})
-    if (st) cudaStreamDestroy(st);
-  if (s->pool_base) cudaFree(s->pool_base);
+  dev_free(s->pool_base);
   delete s;
 }
+
+Req* find_req(ogs_server_s* s, int64_t id) {  // s->mu held
+  if (id < 0 || id >= static_cast<int64_t>(s->all.size())) return nullptr;
+  return s->all[id].get();
+}
+
+bool final_state(int st) { return st == kDone || st == kCancelled; }
 
 }  // namespace
 }  // namespace ogsgb
@@ -323,19 +417,26 @@ ogs_status ogs_server_create(ogs_server* out, const ogs_server_config* cfg) {
   ogs_server_s* s = new (std::nothrow) ogs_server_s();
   if (!s) return set_error(OGS_ENOMEM, "ogs_server_create: out of host memory");
   s->cfg = *cfg;
-  cudaGetDevice(&s->device);
-  cudaError_t e = cudaMalloc(&s->pool_base, static_cast<size_t>(cfg->field_budget_bytes));
-  if (e == cudaSuccess) {
-    s->pool.reset(static_cast<size_t>(cfg->field_budget_bytes));
-    for (cudaStream_t* st : {&s->copy_in, &s->copy_out, &s->compute[0], &s->compute[1]})
+  cudaError_t e = cudaGetDevice(&s->device);
+  if (e == cudaSuccess) e = dev_malloc(&s->pool_base, static_cast<size_t>(cfg->field_budget_bytes));
+  if (e == cudaSuccess) s->pool.reset(static_cast<size_t>(cfg->field_budget_bytes));
+  for (Lane& l : s->lanes) {
+    for (cudaStream_t* st : {&l.in, &l.compute, &l.out})
       if (e == cudaSuccess) e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.copied, cudaEventDisableTiming);
   }
-  s->slots.resize(16);
-  for (TableSlot& t : s->slots) {
-    if (e == cudaSuccess) e = cudaMalloc(&t.d_entries, sizeof(BatchEntry) * cfg->max_batch);
-    if (e == cudaSuccess) e = cudaMalloc(&t.d_starts, sizeof(int64_t) * (cfg->max_batch + 1));
-    if (e == cudaSuccess) e = cudaMallocHost(&t.h_entries, sizeof(BatchEntry) * cfg->max_batch);
-    if (e == cudaSuccess) e = cudaMallocHost(&t.h_starts, sizeof(int64_t) * (cfg->max_batch + 1));
+  // the launch tables of all slots: entries then starts, 256-byte aligned
+  const size_t eb = (sizeof(BatchEntry) * cfg->max_batch + 255) / 256 * 256;
+  const size_t sb = (sizeof(int64_t) * (cfg->max_batch + 1) + 255) / 256 * 256;
+  if (e == cudaSuccess) e = dev_malloc(&s->d_tables, kTableSlots * (eb + sb));
+  if (e == cudaSuccess) e = host_malloc(&s->h_tables, kTableSlots * (eb + sb));
+  if (e == cudaSuccess) s->slots.resize(kTableSlots);
+  for (size_t j = 0; j < s->slots.size(); ++j) {
+    TableSlot& t = s->slots[j];
+    t.d_entries = reinterpret_cast<BatchEntry*>(s->d_tables + j * (eb + sb));
+    t.d_starts = reinterpret_cast<int64_t*>(s->d_tables + j * (eb + sb) + eb);
+    t.h_entries = reinterpret_cast<BatchEntry*>(s->h_tables + j * (eb + sb));
+    t.h_starts = reinterpret_cast<int64_t*>(s->h_tables + j * (eb + sb) + eb);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.done, cudaEventDisableTiming);
   }
   if (e != cudaSuccess) {
@@ -344,7 +445,12 @@ ogs_status ogs_server_create(ogs_server* out, const ogs_server_config* cfg) {
     return set_error(e == cudaErrorMemoryAllocation ? OGS_ENOMEM : OGS_EDEVICE,
                      std::string("ogs_server_create: ") + cudaGetErrorString(e));
   }
-  s->worker = std::thread(worker_loop, s);
+  try {
+    s->worker = std::thread(worker_loop, s);
+  } catch (const std::exception&) {
+    destroy(s);
+    return set_error(OGS_ENOMEM, "ogs_server_create: cannot start the worker thread");
+  }
   *out = s;
   return OGS_OK;
 }
@@ -353,6 +459,7 @@ ogs_status ogs_server_add_mesh(ogs_server s, ogs_handle h, int* mesh_id) {
   if (!s || !h || !mesh_id) return set_error(OGS_EINVAL, "ogs_server_add_mesh: NULL argument");
   if (h->host_only || h->device != s->device)
     return set_error(OGS_EINVAL, "ogs_server_add_mesh: the handle must live on the server's device");
+  if (h->gslib) return set_error(OGS_EINVAL, "ogs_server_add_mesh: handle was made by ogs_gslib_setup");
   if (!h->distinct_cols)
     return set_error(OGS_EINVAL, "ogs_server_add_mesh: a local node appears in two rows of this operator's map");
   std::lock_guard<std::mutex> g(s->mu);
@@ -367,15 +474,18 @@ ogs_status ogs_server_submit(ogs_server s, const ogs_server_request* r, double a
   if (!q) return set_error(OGS_ENOMEM, "ogs_server_submit: out of host memory");
   {
     std::lock_guard<std::mutex> g(s->mu);
+    if (s->stop.load()) return set_error(OGS_EINVAL, "ogs_server_submit: the server is shutting down");
     if (r->mesh < 0 || r->mesh >= static_cast<int>(s->meshes.size()))
       return set_error(OGS_EINVAL, "ogs_server_submit: unknown mesh");
     if (r->type < OGS_FLOAT || r->type > OGS_INT64 || r->op < OGS_ADD || r->op > OGS_MIN || r->k < 1 ||
         r->trans < OGS_SYM || r->trans > OGS_TRANS || !r->host)
       return set_error(OGS_EINVAL, "ogs_server_submit: bad request");
-    q->r = *r;
-    q->bytes = static_cast<size_t>(s->meshes[r->mesh]->N) * r->k * tsize(r->type);
-    if (q->bytes > static_cast<size_t>(s->cfg.field_budget_bytes))
+    const size_t node_bytes = static_cast<size_t>(r->k) * type_size(r->type);
+    const size_t n = static_cast<size_t>(s->meshes[r->mesh]->N);
+    if (n > 0 && node_bytes > static_cast<size_t>(s->cfg.field_budget_bytes) / n)
       return set_error(OGS_ERANGE, "ogs_server_submit: the field is larger than the whole budget");
+    q->r = *r;
+    q->bytes = n * node_bytes;
     q->t_arrival = arrival > 0 ? arrival : now_s();
     q->id = static_cast<int64_t>(s->all.size());
     if (id) *id = q->id;
@@ -389,19 +499,52 @@ ogs_status ogs_server_submit(ogs_server s, const ogs_server_request* r, double a
 
 double ogs_server_clock(void) { return now_s(); }
 
-ogs_status ogs_server_wait(ogs_server s, int64_t id) {
+ogs_status ogs_server_wait_for(ogs_server s, int64_t id, double timeout_s) {
   if (!s) return set_error(OGS_EINVAL, "ogs_server_wait: NULL server");
-  Req* q;
-  {
-    std::lock_guard<std::mutex> g(s->mu);
-    if (id < 0 || id >= static_cast<int64_t>(s->all.size())) return set_error(OGS_EINVAL, "ogs_server_wait: unknown id");
-    q = s->all[id].get();
-  }
+  const auto deadline = std::chrono::steady_clock::now() +
+                        std::chrono::duration_cast<std::chrono::steady_clock::duration>(
+                            std::chrono::duration<double>(timeout_s > 0 ? timeout_s : 0.0));
   std::unique_lock<std::mutex> lk(s->mu);
-  while (q->state.load() != 2) {
+  Req* q = find_req(s, id);
+  if (!q) return set_error(OGS_EINVAL, "ogs_server_wait: unknown id");
+  while (!final_state(q->state.load())) {
     if (!s->error.empty()) return set_error(OGS_EDEVICE, "ogs_server: " + s->error);
+    if (timeout_s >= 0 && std::chrono::steady_clock::now() >= deadline)
+      return set_error(OGS_ETIMEOUT, "ogs_server_wait: request " + std::to_string(id) + " still running");
     s->cv.wait_for(lk, std::chrono::milliseconds(1));
   }
+  return OGS_OK;
+}
+
+ogs_status ogs_server_wait(ogs_server s, int64_t id) { return ogs_server_wait_for(s, id, -1.0); }
+
+ogs_status ogs_server_cancel(ogs_server s, int64_t id, int* cancelled) {
+  if (!s) return set_error(OGS_EINVAL, "ogs_server_cancel: NULL server");
+  bool done_now = false;
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    Req* q = find_req(s, id);
+    if (!q) return set_error(OGS_EINVAL, "ogs_server_cancel: unknown id");
+    if (q->state.load() == kPending) {
+      s->pending.erase(std::find(s->pending.begin(), s->pending.end(), q));
+      q->state.store(kCancelled);
+      done_now = true;
+    }
+  }
+  if (done_now) {
+    s->completed.fetch_add(1);
+    s->cv.notify_all();
+  }
+  if (cancelled) *cancelled = done_now ? 1 : 0;
+  return OGS_OK;
+}
+
+ogs_status ogs_server_state(ogs_server s, int64_t id, int* state) {
+  if (!s || !state) return set_error(OGS_EINVAL, "ogs_server_state: NULL argument");
+  std::lock_guard<std::mutex> g(s->mu);
+  Req* q = find_req(s, id);
+  if (!q) return set_error(OGS_EINVAL, "ogs_server_state: unknown id");
+  *state = q->state.load();
   return OGS_OK;
 }
 
@@ -415,17 +558,24 @@ ogs_status ogs_server_drain(ogs_server s) {
   return OGS_OK;
 }
 
-ogs_status ogs_server_latencies(ogs_server s, int64_t first, int64_t n, double* arrival, double* done) {
-  if (!s) return set_error(OGS_EINVAL, "ogs_server_latencies: NULL server");
+ogs_status ogs_server_times(ogs_server s, int64_t first, int64_t n, double* arrival, double* launched,
+                            double* done) {
+  if (!s) return set_error(OGS_EINVAL, "ogs_server_times: NULL server");
   std::lock_guard<std::mutex> g(s->mu);
   if (first < 0 || n < 0 || first + n > static_cast<int64_t>(s->all.size()))
-    return set_error(OGS_EINVAL, "ogs_server_latencies: range out of bounds");
+    return set_error(OGS_EINVAL, "ogs_server_times: range out of bounds");
   for (int64_t i = 0; i < n; ++i) {
     const Req* q = s->all[first + i].get();
+    const int st = q->state.load();
     if (arrival) arrival[i] = q->t_arrival;
-    if (done) done[i] = q->state.load() == 2 ? q->t_done : -1.0;
+    if (launched) launched[i] = st == kPending || st == kCancelled ? -1.0 : q->t_launch;
+    if (done) done[i] = st == kDone ? q->t_done : -1.0;
   }
   return OGS_OK;
+}
+
+ogs_status ogs_server_latencies(ogs_server s, int64_t first, int64_t n, double* arrival, double* done) {
+  return ogs_server_times(s, first, n, arrival, nullptr, done);
 }
 
 ogs_status ogs_server_counters(ogs_server s, int64_t* launches, int64_t* batched_requests) {

@@ -470,8 +470,8 @@ void release_device(ogs_handle_s* h) {
   if (h->copy_in) cudaStreamDestroy(static_cast<cudaStream_t>(h->copy_in));
   if (h->copy_out) cudaStreamDestroy(static_cast<cudaStream_t>(h->copy_out));
   h->copy_in = h->copy_out = nullptr;
-  if (h->arena) cudaFree(h->arena);
-  if (h->stage) cudaFree(h->stage);
+  if (h->arena) dev_free(h->arena);
+  if (h->stage) dev_free(h->stage);
   h->arena = nullptr;
   h->stage = nullptr;
   h->arena_bytes = h->stage_bytes = 0;
@@ -515,7 +515,7 @@ ogs_status upload_layout(ogs_handle_s* h) {
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return set_error(OGS_EDEVICE, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
   char* base = nullptr;
-  e = cudaMalloc(reinterpret_cast<void**>(&base), total);
+  e = dev_malloc(reinterpret_cast<void**>(&base), total);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return set_error(e == cudaErrorMemoryAllocation ? OGS_ENOMEM : OGS_EDEVICE,
@@ -535,7 +535,7 @@ ogs_status upload_layout(ogs_handle_s* h) {
     if (!p.bytes) continue;
     e = cudaMemcpy(base + p.off, p.src, p.bytes, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
-      cudaFree(base);
+      dev_free(base);
       return set_error(OGS_EDEVICE, std::string("cudaMemcpy of maps: ") + cudaGetErrorString(e));
     }
   }

@@ -195,6 +195,15 @@ class ogs_t:
             raise OgsError(_lib.OGS_EINVAL, "ogs handle is not set up")
         return self._h
 
+    def ReserveHost(self, k, dtype=Double):
+        """Reserve the staging of the host-buffer calls for fields of k
+        components of dtype (a Type or numpy dtype): later host-buffer calls no
+        larger allocate nothing (no reference counterpart; the reference
+        allocates exchange buffers in every call, libs/ogs/ogs.cpp:53)."""
+        t = dtype if isinstance(dtype, Type) else _NP_TYPES[np.dtype(dtype)]
+        check(lib().ogs_reserve_host(self.handle, int(k), int(t)))
+        return self
+
     # ---- GatherScatter (include/ogs.hpp:232-265) ----
     def GatherScatter(self, v, k, op=Add, trans=Sym, stream=None):
         t = _type_of(v)
@@ -361,17 +370,37 @@ class ogs_server_t:
     def clock() -> float:
         return float(lib().ogs_server_clock())
 
-    def wait(self, rid: int):
-        check(lib().ogs_server_wait(self._s, int(rid)))
+    def wait(self, rid: int, timeout: float | None = None):
+        """Until the request is done or cancelled; with a timeout (seconds),
+        OgsError(OGS_ETIMEOUT) when it runs out."""
+        if timeout is None:
+            check(lib().ogs_server_wait(self._s, int(rid)))
+        else:
+            check(lib().ogs_server_wait_for(self._s, int(rid), float(timeout)))
+
+    def cancel(self, rid: int) -> bool:
+        """Withdraw a request not admitted yet; False when it already runs or ran."""
+        c = C.c_int()
+        check(lib().ogs_server_cancel(self._s, int(rid), C.byref(c)))
+        return bool(c.value)
+
+    PENDING, ADMITTED, DONE, CANCELLED = range(4)
+
+    def state(self, rid: int) -> int:
+        st = C.c_int()
+        check(lib().ogs_server_state(self._s, int(rid), C.byref(st)))
+        return st.value
 
     def drain(self):
         check(lib().ogs_server_drain(self._s))
 
-    def times(self, first: int, n: int):
+    def times(self, first: int, n: int, launched: bool = False):
+        """(arrival, done) or, with launched=True, (arrival, launched, done)."""
         a = np.zeros(n)
+        lt = np.zeros(n)
         d = np.zeros(n)
-        check(lib().ogs_server_latencies(self._s, int(first), int(n), a.ctypes.data, d.ctypes.data))
-        return a, d
+        check(lib().ogs_server_times(self._s, int(first), int(n), a.ctypes.data, lt.ctypes.data, d.ctypes.data))
+        return (a, lt, d) if launched else (a, d)
 
     def counters(self):
         l, b = C.c_int64(), C.c_int64()

@@ -294,6 +294,14 @@ class ogs_t {
   template <typename V, typename G>
   void ScatterFinish(V, G, const int, const Transpose) {}
 
+  /* No reference counterpart: reserve the staging of the host-buffer
+   * (memory<T>) overloads for k components of T, so that later calls of no
+   * larger size allocate nothing (ogs_reserve_host). */
+  template <typename T>
+  void ReserveHost(const int k) {
+    check(ogs_reserve_host(h_, k, ogsType<T>::get()));
+  }
+
   ogs_handle handle() const { return h_; }
 
  private:

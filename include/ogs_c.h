@@ -15,9 +15,11 @@
  * failure (the reference aborts with LIBP_ABORT, include/utils.hpp:57-76).
  *
  * Operations are asynchronous on `stream` unless the name ends in _host.  A
- * handle is immutable after setup, so calls on one handle from several
- * streams are safe, except the _host calls, which share the handle's
- * device staging buffer and must not overlap one another.
+ * handle's maps are immutable after setup, so device-buffer calls on one
+ * handle from several streams and threads are safe.  The _host calls share
+ * the handle's device staging buffer: a lock in the handle serialises them
+ * (each returns only after its stream has synchronised), and they allocate
+ * that buffer on first use unless ogs_reserve_host made it at setup time.
  */
 #ifndef OGS_C_H
 #define OGS_C_H
@@ -36,7 +38,7 @@ typedef enum {
   OGS_EINVAL = 1,    /* bad argument or option set */
   OGS_ENOMEM = 2,    /* host or device allocation failed */
   OGS_EDEVICE = 3,   /* CUDA runtime error (message in ogs_last_error_string) */
-  OGS_ETIMEOUT = 4,  /* reserved */
+  OGS_ETIMEOUT = 4,  /* a bounded wait ran out (ogs_server_wait_for) */
   OGS_ERANGE = 5,    /* sizes beyond 32-bit device indices or a stated limit */
   OGS_EUNDEFINED = 6 /* Gather/Scatter on a handle whose gather is not well-defined */
 } ogs_status;
@@ -136,6 +138,15 @@ ogs_status ogs_gather_host(ogs_handle h, void *gv, const void *v, int k, int typ
                            int trans, void *stream);
 ogs_status ogs_scatter_host(ogs_handle h, void *v, const void *gv, int k, int type, int trans,
                             void *stream);
+
+/* Reserve the device staging buffer and the copy streams and events of the
+ * _host calls for fields of k components of `type`, so that no later _host
+ * call on this handle with a field no larger (k*sizeof) allocates anything
+ * (the reference allocates its exchange buffers in every call,
+ * libs/ogs/ogs.cpp:53).  Covers GatherScatter, Gather and Scatter.  Calling
+ * it again with a larger field grows the buffer; with a smaller one it does
+ * nothing.  OGS_ENOMEM leaves the handle usable, without a buffer. */
+ogs_status ogs_reserve_host(ogs_handle h, int k, int type);
 
 /* ogs_gather_scatter_host without any device allocation.  No counterpart in
  * the reference: it exists for callers that must not have a library allocate
@@ -244,14 +255,17 @@ ogs_status ogs_batch_free(ogs_batch b);
 /* ---- Served gather-scatter: resident meshes, continuous batching ----
  * No reference counterpart.  Requests name a resident mesh and carry a host
  * field (k interleaved components per node), gather-scattered in place with
- * the request's op and transpose.  A worker thread admits pending requests in
- * arrival order while a device buffer for the field fits in the budget and an
- * in-flight slot is free, copies them in, runs everything admitted since its
- * last turn as one batched launch per value type (alternating between two
- * compute streams, so batches overlap on the GPU), copies results back and
- * retires them.  Each result equals ogs_gather_scatter_host of that request
- * alone, bit for bit.  Submit from any thread; the host field must stay valid
- * and untouched until the request completes. */
+ * the request's op and transpose.  A worker thread, which never blocks on the
+ * GPU, admits pending requests in arrival order -- skipping, within a window,
+ * those whose device buffer does not fit the budget yet, with a bound on how
+ * often one may be passed over -- and runs everything admitted since its last
+ * turn as one batched launch per value type.  Small and large fields travel
+ * on separate copy and compute streams, so small requests do not queue
+ * behind a large one's copies, and requests arriving while others run are
+ * launched at once beside them.  Each result equals ogs_gather_scatter_host
+ * of that request alone, bit for bit.  Submit from any thread; the host field
+ * must stay valid and untouched until the request completes or is
+ * cancelled. */
 typedef struct ogs_server_s *ogs_server;
 typedef struct {
   int64_t field_budget_bytes; /* device memory for request fields (the HBM budget) */
@@ -273,14 +287,39 @@ ogs_status ogs_server_add_mesh(ogs_server s, ogs_handle h, int *mesh_id);
 /* arrival: time on ogs_server_clock() the request arrived, or 0 for now. */
 ogs_status ogs_server_submit(ogs_server s, const ogs_server_request *r, double arrival, int64_t *id);
 double ogs_server_clock(void);
+/* Until the request is done or cancelled (OGS_EDEVICE if the server failed). */
 ogs_status ogs_server_wait(ogs_server s, int64_t id);
+/* The same, giving up after timeout_s seconds with OGS_ETIMEOUT (the request
+ * carries on; wait again or cancel it). */
+ogs_status ogs_server_wait_for(ogs_server s, int64_t id, double timeout_s);
+/* Withdraw a request that has not been admitted yet: *cancelled = 1 and it
+ * never runs (its host field is not touched); *cancelled = 0 when it is
+ * already running or done, and it completes normally. */
+ogs_status ogs_server_cancel(ogs_server s, int64_t id, int *cancelled);
+/* 0 pending, 1 admitted (on the GPU), 2 done, 3 cancelled. */
+ogs_status ogs_server_state(ogs_server s, int64_t id, int *state);
+/* Until every submitted request is done or cancelled. */
 ogs_status ogs_server_drain(ogs_server s);
 /* Arrival and completion times (ogs_server_clock seconds; -1 = not done) of
  * requests first..first+n-1. */
 ogs_status ogs_server_latencies(ogs_server s, int64_t first, int64_t n, double *arrival, double *done);
+/* The same with the time each request's launch was enqueued (-1 = not yet);
+ * any pointer may be NULL. */
+ogs_status ogs_server_times(ogs_server s, int64_t first, int64_t n, double *arrival, double *launched,
+                            double *done);
 ogs_status ogs_server_counters(ogs_server s, int64_t *launches, int64_t *batched_requests);
 /* Finishes outstanding requests, then releases the server. */
 ogs_status ogs_server_free(ogs_server s);
+
+/* ---- Testing hooks (no reference counterpart) ----
+ * Every device and page-locked host allocation of the library is counted;
+ * ogs_debug_fail_alloc(n) makes the n-th allocation from now fail as if the
+ * memory were exhausted (n = 0 turns it off), so the OGS_ENOMEM paths can be
+ * tested without exhausting a GPU.  ogs_debug_allocations reports the blocks
+ * and bytes the library holds (any pointer may be NULL). */
+ogs_status ogs_debug_fail_alloc(int64_t nth);
+ogs_status ogs_debug_allocations(int64_t *device_blocks, int64_t *device_bytes, int64_t *host_blocks,
+                                 int64_t *host_bytes);
 
 /* Message of the calling thread's last failed call ("" if none). */
 const char *ogs_last_error_string(void);

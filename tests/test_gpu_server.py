@@ -94,3 +94,103 @@ def test_server_rejects_bad_requests(cuda):
         server.submit(m, np.zeros(ids.size * 1000), 1000)  # larger than the whole budget
     assert e.value.status == _lib.OGS_ERANGE
     server.Free()
+
+
+def _pinned(v):
+    return torch.from_numpy(v.copy()).pin_memory()
+
+
+def _wait_state(server, rid, want, limit_s=10.0):
+    t0 = server.clock()
+    while server.state(rid) != want:
+        assert server.clock() - t0 < limit_s, f"request {rid} never reached state {want}"
+
+
+def test_request_arriving_while_a_batch_runs_overlaps_it(cuda, oracle_mod):
+    """Continuous batching: a small request submitted while a large one is on
+    the GPU is launched before the large one retires, finishes first (its
+    copies do not queue behind the large field's), and both results equal
+    the requests run alone."""
+    big_ids = mesh.box_ids(24, 24, 24, 5)   # 2,985,984 nodes x k=8 fp64: 191 MB each way
+    small_ids = mesh.box_ids(4, 4, 4, 2)
+    gb = ogs.ogs_t().Setup(big_ids.size, big_ids.copy())
+    gs = ogs.ogs_t().Setup(small_ids.size, small_ids.copy())
+    server = ogs.ogs_server_t(field_budget_bytes=1 << 30, max_inflight=16, max_batch=8)
+    mb, ms = server.add_mesh(gb), server.add_mesh(gs)
+    vb = values(8 * gb.N, np.float64, "add", seed=71)
+    vs = values(2 * gs.N, np.float64, "max", seed=72)
+    hb, hs = _pinned(vb), _pinned(vs)
+    rb = server.submit(mb, hb, 8)
+    _wait_state(server, rb, server.ADMITTED)
+    rs = server.submit(ms, hs, 2, ogs.Max)
+    server.wait(rs)
+    server.wait(rb)
+    a, launched, done = server.times(0, 2, launched=True)
+    assert launched[1] < done[0], "the later request waited for the running batch to retire"
+    assert done[1] < done[0], "the small request finished after the large one"
+    for g, v, h, k, op in ((gb, vb, hb, 8, ogs.Add), (gs, vs, hs, 2, ogs.Max)):
+        alone = v.copy()
+        g.GatherScatter(alone, k, op, ogs.Sym)
+        assert same_bits(h.numpy(), alone)
+    ref = oracle_mod.OracleOgs(small_ids.copy(), "unsigned")
+    assert same_bits(hs.numpy(), ref.gather_scatter(vs.copy(), 2, "max", "sym"))
+    server.Free()
+
+
+def test_admission_lets_small_requests_pass_one_that_does_not_fit(cuda):
+    """With the budget held by one large field, a second large request waits;
+    a small request submitted after it is admitted and launched first."""
+    big_ids = mesh.box_ids(24, 24, 24, 4)   # 1,728,000 nodes x k=4 fp64 = 55.3 MB
+    small_ids = mesh.box_ids(3, 3, 3, 2)
+    gb = ogs.ogs_t().Setup(big_ids.size, big_ids.copy())
+    gs = ogs.ogs_t().Setup(small_ids.size, small_ids.copy())
+    big_bytes = 4 * 8 * gb.N
+    server = ogs.ogs_server_t(field_budget_bytes=big_bytes + (4 << 20), max_inflight=16, max_batch=8)
+    mb, ms = server.add_mesh(gb), server.add_mesh(gs)
+    vb1, vb2 = values(4 * gb.N, np.float64, "add", seed=81), values(4 * gb.N, np.float64, "add", seed=82)
+    vs = values(gs.N, np.float64, "add", seed=83)
+    h1, h2, h3 = _pinned(vb1), _pinned(vb2), _pinned(vs)
+    r1 = server.submit(mb, h1, 4)
+    r2 = server.submit(mb, h2, 4)
+    r3 = server.submit(ms, h3, 1)
+    server.drain()
+    a, launched, done = server.times(0, 3, launched=True)
+    assert launched[2] < launched[1], "the small request waited behind the large one that did not fit"
+    for g, v, h, k in ((gb, vb1, h1, 4), (gb, vb2, h2, 4), (gs, vs, h3, 1)):
+        alone = v.copy()
+        g.GatherScatter(alone, k, ogs.Add, ogs.Sym)
+        assert same_bits(h.numpy(), alone)
+    assert [server.state(r) for r in (r1, r2, r3)] == [server.DONE] * 3
+    server.Free()
+
+
+def test_cancel_pending_request_and_bounded_wait(cuda):
+    """A request that cannot be admitted yet can be withdrawn (its field is
+    never touched); a bounded wait on a running request returns OGS_ETIMEOUT
+    and the request still completes."""
+    from dawgs_gb300 import _lib
+    big_ids = mesh.box_ids(24, 24, 24, 5)
+    gb = ogs.ogs_t().Setup(big_ids.size, big_ids.copy())
+    big_bytes = 8 * 8 * gb.N
+    server = ogs.ogs_server_t(field_budget_bytes=big_bytes, max_inflight=16, max_batch=8)
+    m = server.add_mesh(gb)
+    v1, v2 = values(8 * gb.N, np.float64, "add", seed=91), values(8 * gb.N, np.float64, "add", seed=92)
+    h1, h2 = _pinned(v1), _pinned(v2)
+    r1 = server.submit(m, h1, 8)
+    r2 = server.submit(m, h2, 8)   # the budget holds one of the two
+    assert server.cancel(r2) is True
+    assert server.state(r2) == server.CANCELLED
+    with pytest.raises(_lib.OgsError) as e:
+        server.wait(r1, timeout=0.0)
+    assert e.value.status == _lib.OGS_ETIMEOUT
+    server.wait(r1, timeout=60.0)
+    server.wait(r2)          # a cancelled request is final
+    assert server.cancel(r1) is False
+    server.drain()
+    assert same_bits(h2.numpy(), v2)  # never ran
+    alone = v1.copy()
+    gb.GatherScatter(alone, 8, ogs.Add, ogs.Sym)
+    assert same_bits(h1.numpy(), alone)
+    _, launched, done = server.times(0, 2, launched=True)
+    assert launched[1] == -1 and done[1] == -1
+    server.Free()
