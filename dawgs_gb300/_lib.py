@@ -56,6 +56,20 @@ SIGNATURES = {
     "ogs_batch_tune": (_i, [_vp, _vp, _vp]),
     "ogs_batch_items": (_i, [_vp, _vp]),
     "ogs_batch_free": (_i, [_vp]),
+    "ogs_halo_setup": (_i, [C.POINTER(_vp), _i64, _vp, _i, _i]),
+    "ogs_halo_setup_maps": (_i, [C.POINTER(_vp), _i64, _i64, _i64, _vp, _vp, _vp, _vp, _i64, _u]),
+    "ogs_halo_setup_from_gather": (_i, [C.POINTER(_vp), _i64, _i64, _i64, _i64]),
+    "ogs_halo_free": (_i, [_vp]),
+    "ogs_halo_get_counts": (_i, [_vp, _vp]),
+    "ogs_halo_reserve": (_i, [_vp, _i, _i, C.POINTER(_vp)]),
+    "ogs_halo_exchange": (_i, [_vp, _vp, _i, _i, _vp, _vp]),
+    "ogs_halo_exchange_start": (_i, [_vp, _vp, _i, _i, _vp, _vp]),
+    "ogs_halo_exchange_finish": (_i, [_vp, _vp, _i, _i, _vp, _vp]),
+    "ogs_halo_combine": (_i, [_vp, _vp, _i, _i, _vp, _vp]),
+    "ogs_halo_combine_start": (_i, [_vp, _vp, _i, _i, _vp, _vp]),
+    "ogs_halo_combine_finish": (_i, [_vp, _vp, _i, _i, _vp, _vp]),
+    "ogs_halo_exchange_host": (_i, [_vp, _vp, _i, _i, _vp, _vp]),
+    "ogs_halo_combine_host": (_i, [_vp, _vp, _i, _i, _vp, _vp]),
     "ogs_server_create": (_i, [C.POINTER(_vp), _vp]),
     "ogs_server_add_mesh": (_i, [_vp, _vp, _vp]),
     "ogs_server_submit": (_i, [_vp, _vp, C.c_double, _vp]),
@@ -94,6 +108,19 @@ class OgsBatchEntry(C.Structure):
 
 
 BATCH_GRAPH = 1
+
+
+class OgsHaloCounts(C.Structure):
+    _fields_ = [("N", C.c_int64), ("NlocalT", C.c_int64), ("NhaloP", C.c_int64), ("NhaloT", C.c_int64),
+                ("Nhalo", C.c_int64), ("Nrecv", C.c_int64), ("gathered", C.c_int32), ("reserved", C.c_int32)]
+
+
+# ogs_exchange_fn and ogs_exchange
+EXCHANGE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p)
+
+
+class OgsExchange(C.Structure):
+    _fields_ = [("start", EXCHANGE_FN), ("finish", EXCHANGE_FN), ("user", C.c_void_p)]
 
 
 class OgsServerConfig(C.Structure):

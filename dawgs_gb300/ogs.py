@@ -288,6 +288,117 @@ class ogs_t:
                 "phase_rows": [tuple(int(x) for x in s.phase_rows[p]) for p in range(int(s.nphases))]}
 
 
+class halo_t:
+    """libParanumal's halo_t (include/ogs.hpp:346-397; libs/ogs/ogsHalo.cpp):
+    Exchange gives every copy of a halo row its owner's value, Combine gives
+    the owner the sum of all copies.  The exchange between ranks (MPI in the
+    reference) is the caller's: set_exchange(start, finish) with callables
+    (d_buf, k, type, trans, stream) -> status, called around the library's
+    device steps.  At one rank (Setup) the halo has no rows."""
+
+    def __init__(self, platform=None):
+        self._h = None
+        self._x = None
+        self._keep = None
+        self.N = self.Nhalo = self.NlocalT = self.NhaloP = self.NhaloT = self.Nrecv = 0
+        self.gathered_halo = False
+
+    def _adopt(self, h):
+        self.Free()
+        self._h = h
+        c = _lib.OgsHaloCounts()
+        check(lib().ogs_halo_get_counts(h, C.byref(c)))
+        self.N, self.NlocalT, self.NhaloP, self.NhaloT = int(c.N), int(c.NlocalT), int(c.NhaloP), int(c.NhaloT)
+        self.Nhalo, self.Nrecv, self.gathered_halo = int(c.Nhalo), int(c.Nrecv), bool(c.gathered)
+        return self
+
+    # halo_t::Setup, ogsSetup.cpp:55-64 (one rank)
+    def Setup(self, N, ids, comm=None, method=Auto, verbose=False, platform=None):
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        h = C.c_void_p()
+        check(lib().ogs_halo_setup(C.byref(h), int(N), ids.ctypes.data, int(method), int(bool(verbose))))
+        return self._adopt(h)
+
+    def SetupMaps(self, N, NhaloP, rowStartsT, colIdsT, rowStartsN=None, colIdsN=None, Nrecv=0):
+        """A halo over the gatherHalo maps of a multi-rank setup."""
+        rsT = np.ascontiguousarray(rowStartsT, dtype=np.int32)
+        ciT = np.ascontiguousarray(colIdsT, dtype=np.int32)
+        rsN = None if rowStartsN is None else np.ascontiguousarray(rowStartsN, dtype=np.int32)
+        ciN = None if colIdsN is None else np.ascontiguousarray(colIdsN, dtype=np.int32)
+        h = C.c_void_p()
+        check(lib().ogs_halo_setup_maps(C.byref(h), int(N), int(NhaloP), int(rsT.size - 1),
+                                        None if rsN is None else rsN.ctypes.data,
+                                        None if ciN is None or ciN.size == 0 else ciN.ctypes.data,
+                                        rsT.ctypes.data, ciT.ctypes.data if ciT.size else None, int(Nrecv), 0))
+        return self._adopt(h)
+
+    # halo_t::SetupFromGather, ogsSetup.cpp:888-913
+    def SetupFromGather(self, g=None, NlocalT=None, NhaloP=0, NhaloT=0, Nrecv=0):
+        if g is not None:
+            if not g.gather_defined:
+                raise OgsError(_lib.OGS_EUNDEFINED, "Gather operation not well-defined.")
+            NlocalT, NhaloP, NhaloT = g.NlocalT, g.NhaloP, g.NhaloT
+        h = C.c_void_p()
+        check(lib().ogs_halo_setup_from_gather(C.byref(h), int(NlocalT), int(NhaloP), int(NhaloT), int(Nrecv)))
+        return self._adopt(h)
+
+    def set_exchange(self, start=None, finish=None):
+        def wrap(f):
+            if f is None:
+                return _lib.EXCHANGE_FN()
+            return _lib.EXCHANGE_FN(lambda user, buf, k, t, tr, st: int(f(buf or 0, k, t, tr, st) or 0))
+        fs = (wrap(start), wrap(finish))
+        self._keep = fs
+        self._x = _lib.OgsExchange(fs[0], fs[1], None)
+        return self
+
+    def reserve(self, k, dtype=Double) -> int:
+        t = dtype if isinstance(dtype, Type) else _NP_TYPES[np.dtype(dtype)]
+        p = C.c_void_p()
+        check(lib().ogs_halo_reserve(self._h, int(k), int(t), C.byref(p)))
+        return p.value or 0
+
+    def _call(self, name, v, k, stream):
+        x = C.byref(self._x) if self._x is not None else None
+        host = not _is_device(v)
+        fn = getattr(lib(), f"ogs_halo_{name}_host" if host else f"ogs_halo_{name}")
+        check(fn(self._h, _ptr(v), int(k), int(_type_of(v)), x, _stream_of(stream)))
+        return v
+
+    def Exchange(self, v, k, stream=None):
+        return self._call("exchange", v, k, stream)
+
+    def ExchangeStart(self, v, k, stream=None):
+        return self._call("exchange" if not _is_device(v) else "exchange_start", v, k, stream)
+
+    def ExchangeFinish(self, v, k, stream=None):
+        return v if not _is_device(v) else self._call("exchange_finish", v, k, stream)
+
+    def Combine(self, v, k, stream=None):
+        return self._call("combine", v, k, stream)
+
+    def CombineStart(self, v, k, stream=None):
+        return self._call("combine" if not _is_device(v) else "combine_start", v, k, stream)
+
+    def CombineFinish(self, v, k, stream=None):
+        return v if not _is_device(v) else self._call("combine_finish", v, k, stream)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def Free(self):
+        if getattr(self, "_h", None) is not None and _lib._lib is not None:
+            lib().ogs_halo_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.Free()
+        except Exception:
+            pass
+
+
 class ogs_batch_t:
     """Many meshes' GatherScatters in one persistent launch (no reference
     counterpart: dawgs calls ogs_t::GatherScatter once per mesh).

@@ -317,6 +317,117 @@ class ogs_t {
   cudaStream_t stream_ = nullptr;
 };
 
+/* halo_t (include/ogs.hpp:346-397 of the reference; libs/ogs/ogsHalo.cpp).
+ * Setup at one rank checks the ids and has no halo rows; SetupFromGather
+ * takes its counts from an ogs_t.  A multi-rank caller attaches its exchange
+ * (the MPI step) with SetExchange and builds the halo from its gatherHalo maps
+ * through ogs_halo_setup_maps (see ogs_c.h). */
+class halo_t {
+ public:
+  bool gathered_halo = false;
+  dlong N = 0, Nhalo = 0, NlocalT = 0, NhaloP = 0, NhaloT = 0;
+
+  halo_t() = default;
+
+  /* ogsSetup.cpp:55-64 */
+  void Setup(const dlong _N, memory<hlong> ids, comm_t /*comm*/, const Method method, const bool verbose,
+             platform_t& platform) {
+    ogs_halo raw = nullptr;
+    check(ogs_halo_setup(&raw, _N, reinterpret_cast<const int64_t*>(ids.ptr()), static_cast<int>(method),
+                         verbose ? 1 : 0));
+    adopt(raw, platform.stream);
+  }
+  /* ogsSetup.cpp:888-913 */
+  void SetupFromGather(ogs_t& ogs) {
+    if (!ogs.gather_defined) throw exception("Gather operation not well-defined.");
+    ogs_halo raw = nullptr;
+    check(ogs_halo_setup_from_gather(&raw, ogs.NlocalT, ogs.NhaloP, ogs.NhaloT, 0));
+    adopt(raw, stream_);
+  }
+  /* no reference counterpart: the exchange (MPI) step of a multi-rank caller */
+  void SetExchange(const ogs_exchange& x) {
+    x_ = x;
+    has_x_ = true;
+  }
+  void Free() {
+    hp_.reset();
+    h_ = nullptr;
+    N = Nhalo = NlocalT = NhaloP = NhaloT = 0;
+  }
+
+  template <typename T>
+  void Exchange(memory<T> v, const int k) {
+    check(ogs_halo_exchange_host(h_, v.ptr(), k, ogs::ogsType<T>::get(), xp(), stream_));
+  }
+  template <typename T>
+  void Exchange(deviceMemory<T> o_v, const int k) {
+    check(ogs_halo_exchange(h_, o_v.ptr(), k, ogs::ogsType<T>::get(), xp(), stream_));
+  }
+  template <typename T>
+  void ExchangeStart(deviceMemory<T> o_v, const int k) {
+    check(ogs_halo_exchange_start(h_, o_v.ptr(), k, ogs::ogsType<T>::get(), xp(), stream_));
+  }
+  template <typename T>
+  void ExchangeFinish(deviceMemory<T> o_v, const int k) {
+    check(ogs_halo_exchange_finish(h_, o_v.ptr(), k, ogs::ogsType<T>::get(), xp(), stream_));
+  }
+  template <typename T>
+  void ExchangeStart(memory<T> v, const int k) { Exchange(v, k); }
+  template <typename T>
+  void ExchangeFinish(memory<T>, const int) {}
+
+  template <typename T>
+  void Combine(memory<T> v, const int k) {
+    check(ogs_halo_combine_host(h_, v.ptr(), k, ogs::ogsType<T>::get(), xp(), stream_));
+  }
+  template <typename T>
+  void Combine(deviceMemory<T> o_v, const int k) {
+    check(ogs_halo_combine(h_, o_v.ptr(), k, ogs::ogsType<T>::get(), xp(), stream_));
+  }
+  template <typename T>
+  void CombineStart(deviceMemory<T> o_v, const int k) {
+    check(ogs_halo_combine_start(h_, o_v.ptr(), k, ogs::ogsType<T>::get(), xp(), stream_));
+  }
+  template <typename T>
+  void CombineFinish(deviceMemory<T> o_v, const int k) {
+    check(ogs_halo_combine_finish(h_, o_v.ptr(), k, ogs::ogsType<T>::get(), xp(), stream_));
+  }
+  template <typename T>
+  void CombineStart(memory<T> v, const int k) { Combine(v, k); }
+  template <typename T>
+  void CombineFinish(memory<T>, const int) {}
+
+  ogs_halo handle() const { return h_; }
+
+ private:
+  void adopt(ogs_halo raw, cudaStream_t stream) {
+    hp_ = std::shared_ptr<ogs_halo_s>(raw, [](ogs_halo q) { ogs_halo_free(q); });
+    h_ = raw;
+    stream_ = stream;
+    ogs_halo_counts c;
+    check(ogs_halo_get_counts(h_, &c));
+    N = static_cast<dlong>(c.N);
+    Nhalo = static_cast<dlong>(c.Nhalo);
+    NlocalT = static_cast<dlong>(c.NlocalT);
+    NhaloP = static_cast<dlong>(c.NhaloP);
+    NhaloT = static_cast<dlong>(c.NhaloT);
+    gathered_halo = c.gathered != 0;
+  }
+  const ogs_exchange* xp() const { return has_x_ ? &x_ : nullptr; }
+  static void check(ogs_status s) {
+    if (s != OGS_OK) {
+      std::ostringstream os;
+      os << "ogs error " << static_cast<int>(s) << ": " << ogs_last_error_string();
+      throw exception(os.str());
+    }
+  }
+  std::shared_ptr<ogs_halo_s> hp_;
+  ogs_halo h_ = nullptr;
+  cudaStream_t stream_ = nullptr;
+  ogs_exchange x_{};
+  bool has_x_ = false;
+};
+
 }  // namespace ogs
 }  // namespace libp
 

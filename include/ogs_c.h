@@ -207,6 +207,77 @@ ogs_status ogs_setup_maps(ogs_handle *out, int64_t N, int64_t NrowsN, int64_t Nr
 ogs_status ogs_extract(int64_t N, int k, int type, const int32_t *d_ids, const void *d_q, void *d_out,
                        void *stream);
 
+/* ---- halo_t: Exchange and Combine of the halo rows ----
+ * libParanumal's halo_t (include/ogs.hpp:346-397; libs/ogs/ogsHalo.cpp:39-359).
+ * Exchange gives every copy of a halo row its owner's value; Combine gives
+ * the owner the sum over all copies.  The library runs the device steps on
+ * the caller's stream -- the gatherHalo Gather into the halo buffer (or, for
+ * a halo made from a gather, a copy of the gathered vector's halo rows) and
+ * the Scatter back -- and calls the caller's exchange between them: the MPI
+ * step that moves the halo buffer between ranks (ogsExchange_t::Start/Finish).
+ * At one rank the halo has no rows and a NULL exchange is the reference's. */
+typedef struct ogs_halo_s *ogs_halo;
+/* The exchange object: start(user, d_buf, k, type, trans, stream) runs after
+ * the halo buffer's rows [0, NhaloP) (Exchange, trans = OGS_NOTRANS) or
+ * [0, NhaloT) (Combine, OGS_TRANS) are queued on `stream`; finish(...) must
+ * leave rows [NhaloP, NhaloT) holding the owners' values (Exchange) or rows
+ * [0, NhaloP) the sums (Combine) before the Scatter that follows on `stream`.
+ * d_buf has room for k*(NhaloT + Nrecv) values.  Either may be NULL. */
+typedef ogs_status (*ogs_exchange_fn)(void *user, void *d_buf, int k, int type, int trans, void *stream);
+typedef struct {
+  ogs_exchange_fn start, finish;
+  void *user;
+} ogs_exchange;
+typedef struct {
+  int64_t N;        /* entries of the vectors Exchange/Combine act on */
+  int64_t NlocalT;  /* local rows before the halo rows (a halo from a gather) */
+  int64_t NhaloP;   /* halo rows this rank owns */
+  int64_t NhaloT;   /* all halo rows */
+  int64_t Nhalo;    /* NhaloT - NhaloP: rows received from their owners (ogsSetup.cpp:63) */
+  int64_t Nrecv;    /* extra rows of the halo buffer for the exchange's received entries */
+  int32_t gathered; /* made from a gather (halo_t::SetupFromGather) */
+  int32_t reserved;
+} ogs_halo_counts;
+/* halo_t::Setup (ogsSetup.cpp:55-64) at one rank: every nonzero id group must
+ * have exactly one positive member (OGS_EINVAL otherwise, ogsSetup.cpp:286-288);
+ * no group is shared with another rank, so the halo has no rows.  No device
+ * memory is used. */
+ogs_status ogs_halo_setup(ogs_halo *out, int64_t N, const int64_t *ids, int method, int verbose);
+/* A halo over the gatherHalo maps that the reference's multi-rank setup
+ * builds (ogsSetup.cpp:569-776: NhaloP rows with an N member first, NhaloT rows
+ * in all; N maps may be NULL for Unsigned), as in ogs_setup_maps; Nrecv rows of
+ * extra buffer for the exchange.  flags: OGS_SETUP_HOST_ONLY or 0. */
+ogs_status ogs_halo_setup_maps(ogs_halo *out, int64_t N, int64_t NhaloP, int64_t NhaloT,
+                               const int32_t *rowStartsN, const int32_t *colIdsN,
+                               const int32_t *rowStartsT, const int32_t *colIdsT, int64_t Nrecv,
+                               unsigned flags);
+/* halo_t::SetupFromGather (ogsSetup.cpp:888-913): the vectors are gathered
+ * ones, NlocalT local rows then NhaloT halo rows (the NhaloP owned ones first). */
+ogs_status ogs_halo_setup_from_gather(ogs_halo *out, int64_t NlocalT, int64_t NhaloP, int64_t NhaloT,
+                                      int64_t Nrecv);
+ogs_status ogs_halo_free(ogs_halo h);
+ogs_status ogs_halo_get_counts(ogs_halo h, ogs_halo_counts *out);
+/* Reserve the halo buffer for k components of `type` (the calls below then
+ * allocate nothing for fields no larger) and return it (NULL when the halo
+ * has no rows).  The reference allocates it in every Start (ogsHalo.cpp:47). */
+ogs_status ogs_halo_reserve(ogs_halo h, int k, int type, void **d_buf);
+/* Exchange / Combine of a device vector (k interleaved components), with
+ * their Start/Finish halves (ogsHalo.cpp:39-143, 185-303). */
+ogs_status ogs_halo_exchange(ogs_halo h, void *d_v, int k, int type, const ogs_exchange *x, void *stream);
+ogs_status ogs_halo_exchange_start(ogs_halo h, void *d_v, int k, int type, const ogs_exchange *x,
+                                   void *stream);
+ogs_status ogs_halo_exchange_finish(ogs_halo h, void *d_v, int k, int type, const ogs_exchange *x,
+                                    void *stream);
+ogs_status ogs_halo_combine(ogs_halo h, void *d_v, int k, int type, const ogs_exchange *x, void *stream);
+ogs_status ogs_halo_combine_start(ogs_halo h, void *d_v, int k, int type, const ogs_exchange *x,
+                                  void *stream);
+ogs_status ogs_halo_combine_finish(ogs_halo h, void *d_v, int k, int type, const ogs_exchange *x,
+                                   void *stream);
+/* Host-vector forms (ogsHalo.cpp:150-183, 311-355): staged through the
+ * device; return after `stream` has synchronised. */
+ogs_status ogs_halo_exchange_host(ogs_halo h, void *v, int k, int type, const ogs_exchange *x, void *stream);
+ogs_status ogs_halo_combine_host(ogs_halo h, void *v, int k, int type, const ogs_exchange *x, void *stream);
+
 /* ---- gslib-compatible entry points ----
  * gslib (3rdParty/gslib of the reference) is the gather-scatter that dawgs
  * checks ogs against (dawgsGS.cpp:34-105).  These calls give its single-rank

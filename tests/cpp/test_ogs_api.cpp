@@ -109,6 +109,33 @@ int main() {
     sgs.SetupGlobalToLocalMapping(g2l);
     for (dlong n = 0; n < N; ++n)
       if (g2l[n] < 0 || g2l[n] >= sgs.NlocalT) { fails++; break; }
+
+    // halo_t at one rank (ogsHalo.cpp): no halo rows, Exchange and Combine
+    // leave the vector as it is; the ids need one positive member per group
+    ogs::halo_t halo;
+    halo.Setup(N, sids, comm, ogs::Auto, false, platform);
+    o_q.copyFrom(q);
+    halo.Exchange(o_q, 1);
+    halo.CombineStart(o_q, 1);
+    halo.CombineFinish(o_q, 1);
+    o_q.copyTo(qtest);
+    qtest.copyFrom(q);
+    halo.Exchange(qtest, 1);
+    for (dlong n = 0; n < N; ++n)
+      if (qtest[n] != q[n]) { fails++; break; }
+    if (halo.Nhalo != 0 || halo.NhaloT != 0) fails++;
+    ogs::halo_t ghalo;
+    ghalo.SetupFromGather(sgs);
+    ghalo.Exchange(o_gq, 1);
+    threw = false;
+    try {
+      ogs::halo_t bad;
+      bad.Setup(N, ids, comm, ogs::Auto, false, platform);  // every member positive
+    } catch (const libp::exception& e) {
+      threw = true;
+      std::printf("rejected halo ids: %s\n", e.what());
+    }
+    if (!threw) fails++;
   } catch (const std::exception& e) {
     std::printf("exception: %s\n", e.what());
     return 2;

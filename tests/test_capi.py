@@ -21,7 +21,7 @@ def declared_functions():
             continue
         src = open(os.path.join(ROOT, "include", fn)).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-        names += re.findall(r"^\s*(?:const\s+)?[a-z_]+\s*\**\s*(ogs_[a-z_0-9]+)\s*\(", src, flags=re.M)
+        names += re.findall(r"^\s*(?!typedef\b)(?:const\s+)?[a-z_]+\s*\**\s*(ogs_[a-z_0-9]+)\s*\(", src, flags=re.M)
     return names
 
 
