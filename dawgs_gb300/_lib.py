@@ -73,6 +73,7 @@ SIGNATURES = {
     "ogs_server_create": (_i, [C.POINTER(_vp), _vp]),
     "ogs_server_add_mesh": (_i, [_vp, _vp, _vp]),
     "ogs_server_submit": (_i, [_vp, _vp, C.c_double, _vp]),
+    "ogs_server_submit_many": (_i, [_vp, _vp, _vp, _i64, _vp]),
     "ogs_server_clock": (C.c_double, []),
     "ogs_server_wait": (_i, [_vp, _i64]),
     "ogs_server_wait_for": (_i, [_vp, _i64, C.c_double]),

@@ -16,6 +16,10 @@
 //                          wait for the gathers of item i (stage s)
 //                          fold item i from shared memory, store
 //
+// With k > 1 components, a warp runs the k components of a tile one after
+// another as consecutive items, so the tile's column ids are loaded once and
+// carried from item to item.
+//
 // Every lane gathers and later folds its own entries only, so no barrier of
 // any kind is needed: cp.async.wait_group makes a thread's own completed
 // copies visible to it.  Two stages suffice: the stage an iteration refills
@@ -114,33 +118,69 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
   const int K = KL == kK1 ? 1 : f.K;
   const int64_t nw = m.nwtiles;
   const int64_t nitems = nw * K;
-  int64_t i = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + warp;
-  if (i >= nitems) return;
+  const int64_t wid = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + warp;
+  // k = 1: warp w takes items w, w+W, ... (the grid sweeps the mesh front to
+  // back).  k > 1: items are (tile, component) pairs, tile-major, and warp w
+  // takes a contiguous run of them, balanced to one item: the k components
+  // of a tile follow one another in one warp, which loads the tile's
+  // descriptor and column ids once for all of them.  Items are followed as
+  // (tile, component) pairs, advanced without division.
+  int64_t i, step, iend;
+  int tcur, ccur;
+  if (KL == kK1) {
+    i = wid;
+    step = W;
+    iend = nitems;
+    tcur = static_cast<int>(i);
+    ccur = 0;
+  } else {
+    const int64_t q = nitems / W, r = nitems % W;
+    i = wid * q + (wid < r ? wid : r);
+    step = 1;
+    iend = i + q + (wid < r ? 1 : 0);
+    tcur = static_cast<int>(i / K);
+    ccur = static_cast<int>(i - static_cast<int64_t>(tcur) * K);
+  }
+  if (i >= iend) return;
   const bool use_mask = !PLAIN && (pat.gather_n || pat.scatter_n) && m.signed_maps;
   const bool gmask = !PLAIN && pat.gather_n != 0;
   const int smode = PLAIN ? 0 : pat.scatter_n;
   const bool gslib = !PLAIN && pat.gslib != 0;
   const int64_t stride = KL == kKInterleaved ? K : 1;
-  auto tile_of = [&](int64_t item) {
-    return static_cast<int>(KL == kKMany ? item % nw : (KL == kKInterleaved ? item / K : item));
-  };
-  auto comp_of = [&](int64_t item) {
-    return KL == kKMany ? static_cast<int>(item / nw) : (KL == kKInterleaved ? static_cast<int>(item % K) : 0);
+  const int Wi = static_cast<int>(W);
+  // the item after (t, c); `same` tells whether it is another component of tile t
+  auto advance = [&](int t, int c, int& tn, int& cn, bool& same) {
+    if (KL == kK1) {
+      tn = t + Wi;
+      cn = 0;
+      same = false;
+    } else if (c + 1 < K) {
+      tn = t;
+      cn = c + 1;
+      same = true;
+    } else {
+      tn = t + 1;
+      cn = 0;
+      same = false;
+    }
   };
   T* gv = static_cast<T*>(f.gv);
 
-  // prologue: the descriptors of items i, i+W, i+2W in one round trip, the
-  // column ids of i and i+W in the next, then the gathers of item i; the
-  // loop's first pass issues the gathers of i+W at once
-  int tcur = tile_of(i);
-  int tnxt = 0;
-  const bool has1 = i + W < nitems;
+  // prologue: the descriptors of items i, i+1 step, i+2 steps in one round
+  // trip, the column ids of the first two in the next, then the gathers of
+  // item i; the loop's first pass issues the gathers of the next item at once
+  int tnxt = 0, cnxt = 0, tnn = 0, cnn = 0;
+  bool snxt_same = false, snn_same = false;
+  const bool has1 = i + step < iend;
   Tile cur = m.wtiles[tcur];
   Tile nxt{}, nn{};
   if (has1) {
-    tnxt = tile_of(i + W);
-    nxt = m.wtiles[tnxt];
-    if (i + 2 * W < nitems) nn = m.wtiles[tile_of(i + 2 * W)];
+    advance(tcur, ccur, tnxt, cnxt, snxt_same);
+    nxt = snxt_same ? cur : m.wtiles[tnxt];
+    if (i + 2 * step < iend) {
+      advance(tnxt, cnxt, tnn, cnn, snn_same);
+      nn = snn_same ? nxt : m.wtiles[tnn];
+    }
   }
   WarpState scur, snxt;
 #define OGS_A_LOAD(D, TILE, TI, S) warp_load_state<MODE, D>(m.b[D], TILE, m.wemask, TI, use_mask, pat, lane, S)
@@ -148,14 +188,17 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
   OGS_DEGREE_SWITCH(cur.bucket, OGS_A_LOAD_CUR)
 #undef OGS_A_LOAD_CUR
   if (has1) {
+    if (snxt_same) {
+      snxt = scur;
+    } else {
 #define OGS_A_LOAD_NXT(D) OGS_A_LOAD(D, nxt, tnxt, snxt)
-    OGS_DEGREE_SWITCH(nxt.bucket, OGS_A_LOAD_NXT)
+      OGS_DEGREE_SWITCH(nxt.bucket, OGS_A_LOAD_NXT)
 #undef OGS_A_LOAD_NXT
+    }
   }
   {
-    const int k0 = comp_of(i);
-    const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, k0);
-#define OGS_A_ISSUE0(D) async_issue_vals<T, MODE, D>(scur, src, gv, stride, K, k0, gmask, lane, ring)
+    const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, ccur);
+#define OGS_A_ISSUE0(D) async_issue_vals<T, MODE, D>(scur, src, gv, stride, K, ccur, gmask, lane, ring)
     OGS_DEGREE_SWITCH(cur.bucket, OGS_A_ISSUE0)
 #undef OGS_A_ISSUE0
   }
@@ -163,52 +206,62 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
 
   int stage = 0;
   for (;;) {
-    const bool more1 = i + W < nitems;
-    const bool more2 = i + 2 * W < nitems;
+    const bool more1 = i + step < iend;
+    const bool more2 = i + 2 * step < iend;
     const int nstage = stage == kAsyncStages - 1 ? 0 : stage + 1;
     if (more1) {
-      const int k1 = comp_of(i + W);
-      const T* src1 = (MODE == kModeScatter) ? nullptr : field_base<T>(f, k1);
+      const T* src1 = (MODE == kModeScatter) ? nullptr : field_base<T>(f, cnxt);
       T* st1 = ring + nstage * (kWarpSlots * 32);
-#define OGS_A_ISSUE1(D) async_issue_vals<T, MODE, D>(snxt, src1, gv, stride, K, k1, gmask, lane, st1)
+#define OGS_A_ISSUE1(D) async_issue_vals<T, MODE, D>(snxt, src1, gv, stride, K, cnxt, gmask, lane, st1)
       OGS_DEGREE_SWITCH(nxt.bucket, OGS_A_ISSUE1)
 #undef OGS_A_ISSUE1
     }
     cp_async_commit();
     WarpState snn;
     Tile n3{};
-    int tnn = 0;
+    int tn3 = 0, cn3 = 0;
+    bool sn3_same = false;
     if (more2) {
-      tnn = tile_of(i + 2 * W);
+      if (snn_same) {
+        snn = snxt;  // another component of the same tile: its column ids are loaded
+      } else {
 #define OGS_A_LOAD_NN(D) OGS_A_LOAD(D, nn, tnn, snn)
-      OGS_DEGREE_SWITCH(nn.bucket, OGS_A_LOAD_NN)
+        OGS_DEGREE_SWITCH(nn.bucket, OGS_A_LOAD_NN)
 #undef OGS_A_LOAD_NN
-      if (i + 3 * W < nitems) n3 = m.wtiles[tile_of(i + 3 * W)];
+      }
+      if (i + 3 * step < iend) {
+        advance(tnn, cnn, tn3, cn3, sn3_same);
+        n3 = sn3_same ? nn : m.wtiles[tn3];
+      }
     }
     cp_async_wait<1>();  // the gathers of item i are in
     {
-      const int k0 = comp_of(i);
-      T* dst = (MODE == kModeGather) ? nullptr : field_base<T>(f, k0);
+      T* dst = (MODE == kModeGather) ? nullptr : field_base<T>(f, ccur);
       const T* st0 = ring + stage * (kWarpSlots * 32);
       T V[kWarpSlots];
-#define OGS_A_FOLD(D)                                                                            \
-  do {                                                                                           \
-    async_read_vals<T, MODE, D>(scur, gmask, lane, st0, V);                                      \
-    warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, k0, gmask, smode, gslib, lane, V); \
+#define OGS_A_FOLD(D)                                                                              \
+  do {                                                                                             \
+    async_read_vals<T, MODE, D>(scur, gmask, lane, st0, V);                                        \
+    warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, ccur, gmask, smode, gslib, lane, V); \
   } while (0)
       OGS_DEGREE_SWITCH(cur.bucket, OGS_A_FOLD)
 #undef OGS_A_FOLD
     }
     if (!more1) break;
-    i += W;
+    i += step;
     stage = nstage;
     cur = nxt;
     scur = snxt;
     tcur = tnxt;
+    ccur = cnxt;
     nxt = nn;
     snxt = snn;
     tnxt = tnn;
+    cnxt = cnn;
     nn = n3;
+    tnn = tn3;
+    cnn = cn3;
+    snn_same = sn3_same;
   }
   cp_async_wait<0>();
 #undef OGS_A_LOAD

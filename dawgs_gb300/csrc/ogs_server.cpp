@@ -23,8 +23,11 @@
 //              turn instead of blocking the worker.
 // Requests arriving while others are on the GPU are admitted and launched on
 // the next turn, so their copies and kernels overlap the earlier ones'.
-// Latency is completion minus arrival (the submit time, or the arrival time the
-// caller passes).  Every result equals the request's ogs_gather_scatter_host
+// Latency is completion minus arrival: the submit time, or the arrival time
+// the caller passes.  A request whose arrival lies in the future is not
+// admitted before that time, so a caller (a load generator) can hand over a
+// whole schedule of arrivals at once and the server sees each request when it
+// arrives.  Every result equals the request's ogs_gather_scatter_host
 // alone, bit for bit: batching changes where the rows run, not their fold.
 #include <algorithm>
 #include <atomic>
@@ -319,17 +322,25 @@ void retire(ogs_server_s* s, Lane& lane) {
   if (n) s->cv.notify_all();
 }
 
-// Admission pass (s->mu held): requests that fit, in arrival order, within
-// the window.  Every admission counts as a pass-over for each earlier request
-// of the pass that did not fit; one passed over kMaxPassOvers times stops the
-// scan at itself, so it is the next to be admitted once memory frees up.
-void admit(ogs_server_s* s) {
+// Admission pass (s->mu held): requests that have arrived and fit, in
+// submission order, within the window.  Every admission counts as a
+// pass-over for each earlier request of the pass that did not fit; one passed
+// over kMaxPassOvers times stops the scan at itself, so it is the next to be
+// admitted once memory frees up.  Returns the earliest arrival still in the
+// future (0 if none was seen).
+double admit(ogs_server_s* s, double now) {
   int looked = 0;
+  double next = 0;
   std::vector<Req*> blocked;
   for (auto it = s->pending.begin(); it != s->pending.end() && looked < kAdmitWindow;) {
     if (s->inflight.load() >= s->cfg.max_inflight) break;
     Req* q = *it;
     looked++;
+    if (q->t_arrival > now) {  // scheduled, not arrived yet
+      if (next == 0 || q->t_arrival < next) next = q->t_arrival;
+      ++it;
+      continue;
+    }
     Lane& lane = s->lanes[q->bytes <= kSmallBytes ? 0 : 1];
     if (static_cast<int>(lane.ready.size()) < s->cfg.max_batch && s->pool.alloc(q->bytes, &q->off)) {
       it = s->pending.erase(it);
@@ -343,6 +354,7 @@ void admit(ogs_server_s* s) {
     blocked.push_back(q);
     ++it;
   }
+  return next;
 }
 
 void worker_loop(ogs_server_s* s) {
@@ -355,12 +367,22 @@ void worker_loop(ogs_server_s* s) {
       const bool nothing_out = s->lanes[0].outstanding.empty() && s->lanes[1].outstanding.empty();
       const bool nothing_ready = s->lanes[0].ready.empty() && s->lanes[1].ready.empty();
       if (s->pending.empty() && nothing_ready && s->stop.load() && s->inflight.load() == 0) break;
-      admit(s);
+      const double now = now_s();
+      const double next = admit(s, now);
       idle = s->lanes[0].ready.empty() && s->lanes[1].ready.empty();
       if (idle) {
-        // nothing to launch: wait for a submission, or come back soon to
-        // retire what is in flight (which may free budget for the pending)
-        s->cv.wait_for(lk, std::chrono::microseconds(nothing_out ? 500 : 20));
+        // nothing to launch: wait for a submission or the next scheduled
+        // arrival, or come back soon to retire what is in flight (which may
+        // free budget for the pending); an arrival due within 100 us is
+        // waited for by polling, for its admission time
+        double wait_us = nothing_out ? 500 : 20;
+        if (next > 0) wait_us = std::min(wait_us, (next - now) * 1e6);
+        if (wait_us > 100) {
+          s->cv.wait_for(lk, std::chrono::microseconds(static_cast<int64_t>(wait_us)));
+        } else if (next > 0 && wait_us > 0) {
+          lk.unlock();
+          std::this_thread::yield();
+        }
         continue;
       }
     }
@@ -468,33 +490,59 @@ ogs_status ogs_server_add_mesh(ogs_server s, ogs_handle h, int* mesh_id) {
   return OGS_OK;
 }
 
-ogs_status ogs_server_submit(ogs_server s, const ogs_server_request* r, double arrival, int64_t* id) {
-  if (!s || !r) return set_error(OGS_EINVAL, "ogs_server_submit: NULL argument");
-  std::unique_ptr<Req> q(new (std::nothrow) Req());
-  if (!q) return set_error(OGS_ENOMEM, "ogs_server_submit: out of host memory");
+ogs_status ogs_server_submit_many(ogs_server s, const ogs_server_request* rs, const double* arrivals, int64_t n,
+                                  int64_t* first_id) {
+  const char* fn = "ogs_server_submit";
+  if (!s || (!rs && n > 0)) return set_error(OGS_EINVAL, std::string(fn) + ": NULL argument");
+  if (n < 0) return set_error(OGS_EINVAL, std::string(fn) + ": n must be >= 0");
+  std::vector<std::unique_ptr<Req>> qs;
+  try {
+    qs.reserve(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) qs.emplace_back(new Req());
+  } catch (const std::bad_alloc&) {
+    return set_error(OGS_ENOMEM, std::string(fn) + ": out of host memory");
+  }
   {
     std::lock_guard<std::mutex> g(s->mu);
-    if (s->stop.load()) return set_error(OGS_EINVAL, "ogs_server_submit: the server is shutting down");
-    if (r->mesh < 0 || r->mesh >= static_cast<int>(s->meshes.size()))
-      return set_error(OGS_EINVAL, "ogs_server_submit: unknown mesh");
-    if (r->type < OGS_FLOAT || r->type > OGS_INT64 || r->op < OGS_ADD || r->op > OGS_MIN || r->k < 1 ||
-        r->trans < OGS_SYM || r->trans > OGS_TRANS || !r->host)
-      return set_error(OGS_EINVAL, "ogs_server_submit: bad request");
-    const size_t node_bytes = static_cast<size_t>(r->k) * type_size(r->type);
-    const size_t n = static_cast<size_t>(s->meshes[r->mesh]->N);
-    if (n > 0 && node_bytes > static_cast<size_t>(s->cfg.field_budget_bytes) / n)
-      return set_error(OGS_ERANGE, "ogs_server_submit: the field is larger than the whole budget");
-    q->r = *r;
-    q->bytes = n * node_bytes;
-    q->t_arrival = arrival > 0 ? arrival : now_s();
-    q->id = static_cast<int64_t>(s->all.size());
-    if (id) *id = q->id;
-    s->pending.push_back(q.get());
-    s->all.push_back(std::move(q));
+    if (s->stop.load()) return set_error(OGS_EINVAL, std::string(fn) + ": the server is shutting down");
+    // every request is checked before any is queued
+    for (int64_t i = 0; i < n; ++i) {
+      const ogs_server_request* r = &rs[i];
+      if (r->mesh < 0 || r->mesh >= static_cast<int>(s->meshes.size()))
+        return set_error(OGS_EINVAL, std::string(fn) + ": unknown mesh");
+      if (r->type < OGS_FLOAT || r->type > OGS_INT64 || r->op < OGS_ADD || r->op > OGS_MIN || r->k < 1 ||
+          r->trans < OGS_SYM || r->trans > OGS_TRANS || !r->host)
+        return set_error(OGS_EINVAL, std::string(fn) + ": bad request");
+      const size_t node_bytes = static_cast<size_t>(r->k) * type_size(r->type);
+      const size_t nn = static_cast<size_t>(s->meshes[r->mesh]->N);
+      if (nn > 0 && node_bytes > static_cast<size_t>(s->cfg.field_budget_bytes) / nn)
+        return set_error(OGS_ERANGE, std::string(fn) + ": the field is larger than the whole budget");
+    }
+    try {
+      s->all.reserve(s->all.size() + static_cast<size_t>(n));
+    } catch (const std::bad_alloc&) {
+      return set_error(OGS_ENOMEM, std::string(fn) + ": out of host memory");
+    }
+    const double now = now_s();
+    if (first_id) *first_id = static_cast<int64_t>(s->all.size());
+    for (int64_t i = 0; i < n; ++i) {
+      Req* q = qs[i].get();
+      q->r = rs[i];
+      q->bytes = static_cast<size_t>(s->meshes[rs[i].mesh]->N) * static_cast<size_t>(rs[i].k) * type_size(rs[i].type);
+      q->t_arrival = arrivals && arrivals[i] > 0 ? arrivals[i] : now;
+      q->id = static_cast<int64_t>(s->all.size());
+      s->pending.push_back(q);
+      s->all.push_back(std::move(qs[i]));
+    }
   }
-  s->submitted.fetch_add(1);
+  s->submitted.fetch_add(n);
   s->cv.notify_all();
   return OGS_OK;
+}
+
+ogs_status ogs_server_submit(ogs_server s, const ogs_server_request* r, double arrival, int64_t* id) {
+  if (!r) return set_error(OGS_EINVAL, "ogs_server_submit: NULL argument");
+  return ogs_server_submit_many(s, r, &arrival, 1, id);
 }
 
 double ogs_server_clock(void) { return now_s(); }

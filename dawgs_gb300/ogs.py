@@ -477,6 +477,21 @@ class ogs_server_t:
         check(lib().ogs_server_submit(self._s, C.byref(r), float(arrival), C.byref(rid)))
         return rid.value
 
+    def submit_many(self, reqs, arrivals=None) -> int:
+        """reqs: (mesh, host field, k, op, trans) tuples; arrivals: one
+        ogs_server_clock time each (future times are scheduled), or None for
+        now.  Returns the first id; the others follow in order."""
+        n = len(reqs)
+        arr = (_lib.OgsServerRequest * max(n, 1))()
+        for i, (mesh, host, k, op, trans) in enumerate(reqs):
+            arr[i] = _lib.OgsServerRequest(int(mesh), int(_type_of(host)), int(k), int(op), int(trans), 0,
+                                           _ptr(host))
+        a = None if arrivals is None else np.ascontiguousarray(arrivals, dtype=np.float64)
+        first = C.c_int64()
+        check(lib().ogs_server_submit_many(self._s, arr, None if a is None else a.ctypes.data, n,
+                                           C.byref(first)))
+        return first.value
+
     @staticmethod
     def clock() -> float:
         return float(lib().ogs_server_clock())

@@ -355,8 +355,14 @@ typedef struct {
 ogs_status ogs_server_create(ogs_server *out, const ogs_server_config *cfg);
 /* Make a set-up handle resident (the server does not own it). */
 ogs_status ogs_server_add_mesh(ogs_server s, ogs_handle h, int *mesh_id);
-/* arrival: time on ogs_server_clock() the request arrived, or 0 for now. */
+/* arrival: time on ogs_server_clock() the request arrived, or 0 for now; a
+ * time in the future schedules the request: it is not admitted before then
+ * (latency still counts from `arrival`). */
 ogs_status ogs_server_submit(ogs_server s, const ogs_server_request *r, double arrival, int64_t *id);
+/* n requests at once, ids *first_id .. *first_id+n-1; arrivals may be NULL
+ * (all now).  Either every request is queued or none (bad request, OGS_ERANGE). */
+ogs_status ogs_server_submit_many(ogs_server s, const ogs_server_request *rs, const double *arrivals,
+                                  int64_t n, int64_t *first_id);
 double ogs_server_clock(void);
 /* Until the request is done or cancelled (OGS_EDEVICE if the server failed). */
 ogs_status ogs_server_wait(ogs_server s, int64_t id);
