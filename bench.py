@@ -314,7 +314,6 @@ def run_batched(a, dev, L, stream, log=None):
         dofs += g.NgatherGlobal * k
         nlocal += ids.size * k
     batch = ogs.ogs_batch_t([(g, f, k, ogs.Add, ogs.Sym) for g, f, k in zip(handles, fields, ks)], graph=True)
-    grid = batch.tune(stream)
 
     def restore():
         for f, p0 in zip(fields, pristine):
@@ -347,6 +346,14 @@ def run_batched(a, dev, L, stream, log=None):
             L.ogs_gather_scatter(g.handle, f.data_ptr(), k, 1, 0, 0, stream.cuda_stream)
 
     t_plain = time_it(plain, max(a.steps // 2, 5))
+    # every entry in the one persistent launch, as many CTAs as fit
+    batch.set_config(stream=stream)
+    t_persistent = time_it(lambda: batch.GatherScatter(stream), max(a.steps, 10))
+    # the tuner times on scratch copies: the fields must come out untouched
+    restore()
+    tuned = batch.tune(stream, use_cache=False)
+    untouched = all(torch.equal(f, p0) for f, p0 in zip(fields, pristine))
+    again = batch.tune(stream)  # same key: taken from the cache
     t_batch = time_it(lambda: batch.GatherScatter(stream), max(a.steps, 10))
     # results: batched equals plain bit for bit (both from the pristine fields)
     restore()
@@ -357,10 +364,12 @@ def run_batched(a, dev, L, stream, log=None):
     torch.cuda.synchronize(dev)
     same = all(torch.equal(x, y) for x, y in zip(got, fields))
     return {"workload": f"{len(mix)} box meshes, NX,NY,NZ~U[2,16], p~U[1,7], fp64 k~U[1,4], Add Sym",
-            "local_values": int(nlocal), "global_dofs_x_k": int(dofs), "items": batch.items, "grid": grid,
-            "plain_ms": t_plain * 1e3, "batched_ms": t_batch * 1e3,
+            "local_values": int(nlocal), "global_dofs_x_k": int(dofs), "items": batch.items,
+            "tuned": tuned, "second_tune_from_cache": again["from_cache"], "tuner_left_fields_untouched": untouched,
+            "plain_ms": t_plain * 1e3, "batched_ms": t_batch * 1e3, "persistent_only_ms": t_persistent * 1e3,
             "plain_dofs_per_s": dofs / t_plain, "batched_dofs_per_s": dofs / t_batch,
-            "speedup": t_plain / t_batch, "identical_to_plain": bool(same),
+            "speedup": t_plain / t_batch, "speedup_persistent_only": t_plain / t_persistent,
+            "identical_to_plain": bool(same),
             "l2": "working set larger than L2 (no flush)", "graph": True}
 
 

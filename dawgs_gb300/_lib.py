@@ -54,6 +54,11 @@ SIGNATURES = {
     "ogs_batch_set_fields": (_i, [_vp, _vp, _vp]),
     "ogs_batch_gather_scatter": (_i, [_vp, _vp]),
     "ogs_batch_tune": (_i, [_vp, _vp, _vp]),
+    "ogs_batch_tune_ex": (_i, [_vp, _vp, _u, _vp]),
+    "ogs_batch_get_config": (_i, [_vp, _vp]),
+    "ogs_batch_set_config": (_i, [_vp, _vp, _vp]),
+    "ogs_batch_tune_key": (_i, [_i, _i, _i, _vp, _vp, _vp]),
+    "ogs_batch_tune_cache_clear": (_i, []),
     "ogs_batch_items": (_i, [_vp, _vp]),
     "ogs_batch_free": (_i, [_vp]),
     "ogs_halo_setup": (_i, [C.POINTER(_vp), _i64, _vp, _i, _i]),
@@ -109,6 +114,13 @@ class OgsBatchEntry(C.Structure):
 
 
 BATCH_GRAPH = 1
+TUNE_NO_CACHE = 1
+
+
+class OgsBatchConfig(C.Structure):
+    _fields_ = [("block", C.c_int32), ("ctas_per_sm", C.c_int32), ("solo_items", C.c_int64),
+                ("solo_streams", C.c_int32), ("sms", C.c_int32), ("from_cache", C.c_int32),
+                ("reserved", C.c_int32), ("ms", C.c_double)]
 
 
 class OgsHaloCounts(C.Structure):

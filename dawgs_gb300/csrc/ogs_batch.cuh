@@ -4,15 +4,13 @@
 // handle carries, from setup, one 32-byte record per warp tile (WarpRec:
 // column and row arrays of its bucket, first row, degree and row count); the
 // batch adds a prefix table `starts` over the entries' (record, component)
-// items.  Warp w of the grid takes items w, w+W, ..., finds an item's entry by
-// binary search (in shared memory for up to kBatchSmem entries), and runs the
-// same per-warp pipeline as ogs_warp.cuh: the next item's column ids load
-// while the current item's values are gathered, folded and stored.  The k
-// components of one record are neighbouring items, so they run on
-// neighbouring warps at the same time and share the column ids and field
-// sectors through L1/L2.  The fold follows ogsOperator.cpp:311-360 with
-// the entry's op chosen at run time (warp-uniform), so one launch serves
-// entries with different ops.
+// items.  Warp w of the grid takes a contiguous run of items, so a record's k
+// components follow one another in one warp (its column ids are loaded once)
+// and the walk from item to item needs no search, and runs the same per-warp
+// pipeline as ogs_warp.cuh: the next item's column ids load while the
+// current item's values are gathered, folded and stored.  The fold follows
+// ogsOperator.cpp:311-360 with the entry's op chosen at run time
+// (warp-uniform), so one launch serves entries with different ops.
 #pragma once
 
 #include "ogs_warp.cuh"
@@ -50,31 +48,66 @@ __device__ __forceinline__ int batch_entry_of(const int64_t* starts, int n, int6
 // One work item, (entry e, warp record r, component k), reduced to what the
 // fold needs: field, masks, column ids of the record's bucket and its tile.
 struct BatchItem {
+  const WarpRec* recs;
   const int32_t* cols;
   void* v;
   const uint8_t* wemask;
   int32_t K, flags;  // flags: op | gather_n << 4 | scatter_n << 5 | limit_n << 6 | use_mask << 7
-  int32_t r, k;
+  int32_t e, r, k;
   int32_t begin, bucket_count, stride, nP;
 };
 
-__device__ __forceinline__ void batch_item(const BatchEntry* E, const int64_t* st, int n, int64_t i,
-                                           BatchItem& it) {
-  const int e = batch_entry_of(st, n, i);
+__device__ __forceinline__ void batch_load_entry(const BatchEntry* E, int e, BatchItem& it) {
   const BatchEntry& be = E[e];
+  it.recs = be.recs;
   it.v = be.v;
   it.wemask = be.wemask;
   it.K = be.K;
   it.flags = be.op | (be.gather_n << 4) | (be.scatter_n << 5) | (be.limit_n << 6) | (be.use_mask << 7);
-  const int64_t local = i - st[e];
-  it.r = static_cast<int32_t>(local / it.K);
-  it.k = static_cast<int32_t>(local - static_cast<int64_t>(it.r) * it.K);
-  const WarpRec& w = be.recs[it.r];
+  it.e = e;
+}
+
+__device__ __forceinline__ void batch_load_rec(BatchItem& it) {
+  const WarpRec& w = it.recs[it.r];
   it.cols = w.cols;
   it.begin = w.begin;
   it.bucket_count = w.bucket_count;
   it.stride = w.stride;
   it.nP = w.nP;
+}
+
+// The item at global index i (one binary search; once per warp).
+__device__ __forceinline__ void batch_item_at(const BatchEntry* E, const int64_t* st, int n, int64_t i,
+                                              BatchItem& it) {
+  batch_load_entry(E, batch_entry_of(st, n, i), it);
+  const int64_t local = i - st[it.e];
+  it.r = static_cast<int32_t>(local / it.K);
+  it.k = static_cast<int32_t>(local - static_cast<int64_t>(it.r) * it.K);
+  batch_load_rec(it);
+}
+
+// The item after `a` (global index i_next = a's index + 1): the next
+// component of the same record, the next record, or the first record of the
+// next entry with any.  Returns whether it is the same record.
+__device__ __forceinline__ bool batch_advance(const BatchEntry* E, const int64_t* st, int n, int64_t i_next,
+                                              const BatchItem& a, BatchItem& b) {
+  b = a;
+  if (i_next < st[a.e + 1]) {
+    if (a.k + 1 < a.K) {
+      b.k = a.k + 1;
+      return true;
+    }
+    b.r = a.r + 1;
+    b.k = 0;
+  } else {
+    int e = a.e + 1;
+    while (e < n - 1 && st[e + 1] == st[e]) ++e;  // entries without records
+    batch_load_entry(E, e, b);
+    b.r = 0;
+    b.k = 0;
+  }
+  batch_load_rec(b);
+  return false;
 }
 
 __device__ __forceinline__ void batch_load_state(const BatchItem& it, int lane, WarpState& s) {
@@ -99,30 +132,38 @@ __device__ __forceinline__ void batch_load_state(const BatchItem& it, int lane, 
 #undef OGS_B_LOAD
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kBlock, OGS_BATCH_MINB) ogs_batch_kernel(const BatchEntry* __restrict__ E,
-                                                                          const int64_t* __restrict__ starts,
-                                                                          int n) {
-  __shared__ int64_t s_starts[kBatchSmem + 1];
+// Warp w takes a contiguous run of the (entry, record, component) items,
+// balanced to one item: the k components of a record follow one another in
+// one warp, which loads the record's column ids once for all of them, and the
+// walk from item to item needs no search.  The prefix `starts` is staged in
+// shared memory (dynamic, (n+1) entries) when it fits.
+template <typename T, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, OGS_BATCH_MINB * 256 / BLOCK)
+    ogs_batch_kernel(const BatchEntry* __restrict__ E, const int64_t* __restrict__ starts, int n) {
+  extern __shared__ int64_t s_starts[];
   const bool in_smem = n <= kBatchSmem;
   if (in_smem)
-    for (int j = threadIdx.x; j <= n; j += kBlock) s_starts[j] = starts[j];
+    for (int j = threadIdx.x; j <= n; j += BLOCK) s_starts[j] = starts[j];
   __syncthreads();
   const int64_t* st = in_smem ? s_starts : starts;
   const int64_t nitems = st[n];
   const int lane = static_cast<int>(threadIdx.x) & 31;
-  const int64_t W = static_cast<int64_t>(gridDim.x) * (kBlock / 32);
-  int64_t i = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + (threadIdx.x >> 5);
-  if (i >= nitems) return;
+  const int64_t W = static_cast<int64_t>(gridDim.x) * (BLOCK / 32);
+  const int64_t wid = static_cast<int64_t>(blockIdx.x) * (BLOCK / 32) + (threadIdx.x >> 5);
+  const int64_t q = nitems / W, rem = nitems % W;
+  int64_t i = wid * q + (wid < rem ? wid : rem);
+  const int64_t iend = i + q + (wid < rem ? 1 : 0);
+  if (i >= iend) return;
 
   BatchItem cur, nxt;
-  batch_item(E, st, n, i, cur);
+  batch_item_at(E, st, n, i, cur);
   WarpState scur;
   batch_load_state(cur, lane, scur);
-  if (i + W < nitems) batch_item(E, st, n, i + W, nxt);
+  bool nxt_same = false;
+  if (i + 1 < iend) nxt_same = batch_advance(E, st, n, i + 1, cur, nxt);
 
   for (;;) {
-    const bool more = i + W < nitems;
+    const bool more = i + 1 < iend;
     const int K = cur.K, k = cur.k, d = cur.bucket_count >> 16;
     const bool gmask = (cur.flags >> 4) & 1;
     const int smode = (cur.flags >> 5) & 1;
@@ -133,23 +174,26 @@ __global__ void __launch_bounds__(kBlock, OGS_BATCH_MINB) ogs_batch_kernel(const
 #undef OGS_B_VALS
     WarpState snxt;
     BatchItem nn;
+    bool nn_same = false;
     if (more) {
-      batch_load_state(nxt, lane, snxt);
-      if (i + 2 * W < nitems) batch_item(E, st, n, i + 2 * W, nn);
+      if (nxt_same) snxt = scur;  // another component of the same record
+      else batch_load_state(nxt, lane, snxt);
+      if (i + 2 < iend) nn_same = batch_advance(E, st, n, i + 2, nxt, nn);
     }
 #define OGS_B_FOLD(D) fold_store_rt<T, D>(cur.flags & 15, scur, base, K, K, k, gmask, smode, lane, V)
     OGS_DEGREE_SWITCH(d, OGS_B_FOLD)
 #undef OGS_B_FOLD
     if (!more) break;
-    i += W;
+    i += 1;
     cur = nxt;
     scur = snxt;
     nxt = nn;
+    nxt_same = nn_same;
   }
 }
 
-template <typename T>
-inline int batch_blocks_per_sm(int* sms) {
+template <typename T, int BLOCK>
+inline int batch_blocks_per_sm(int n, int* sms) {
   static DeviceCache bps_cache, sms_cache;
   int dev = 0;
   cudaGetDevice(&dev);
@@ -158,24 +202,34 @@ inline int batch_blocks_per_sm(int* sms) {
     cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
     return s > 0 ? s : 1;
   });
+  (void)n;
+  // occupancy with the largest starts table (the registers decide it)
   return bps_cache.get(dev, [] {
     int bps = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_batch_kernel<T>, kBlock, 0);
+    cudaFuncSetAttribute(ogs_batch_kernel<T, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>((kBatchSmem + 1) * sizeof(int64_t)));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_batch_kernel<T, BLOCK>, BLOCK, 0);
     return bps > 0 ? bps : 1;
   });
 }
 
-// grid <= 0: resident CTAs on every SM.
+// grid <= 0: resident CTAs on every SM; grid > 0: that many CTAs.  block:
+// 128 or 256 threads per CTA.
 template <typename T>
 inline int launch_batch_typed(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid,
-                              void* stream) {
+                              int block, void* stream) {
   if (nitems <= 0) return 0;
   int sms = 0;
-  const int bps = batch_blocks_per_sm<T>(&sms);
+  const int bps = block == 128 ? batch_blocks_per_sm<T, 128>(n, &sms) : batch_blocks_per_sm<T, 256>(n, &sms);
   int64_t g = grid > 0 ? grid : static_cast<int64_t>(bps) * sms;
-  const int64_t need = (nitems + (kBlock / 32) - 1) / (kBlock / 32);
+  const int64_t need = (nitems + (block / 32) - 1) / (block / 32);
   if (g > need) g = need;
-  ogs_batch_kernel<T><<<static_cast<unsigned>(g), kBlock, 0, static_cast<cudaStream_t>(stream)>>>(E, starts, n);
+  const size_t smem = n <= kBatchSmem ? static_cast<size_t>(n + 1) * sizeof(int64_t) : 0;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (block == 128)
+    ogs_batch_kernel<T, 128><<<static_cast<unsigned>(g), 128, smem, st>>>(E, starts, n);
+  else
+    ogs_batch_kernel<T, 256><<<static_cast<unsigned>(g), 256, smem, st>>>(E, starts, n);
   return static_cast<int>(cudaGetLastError());
 }
 

@@ -296,11 +296,16 @@ int launch_f64(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern p
 int launch_i32(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, void* stream);
 int launch_i64(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, void* stream);
 
-// Batched launch over `n` entries (ogs_batch.cuh); grid <= 0 = one full wave.
-int launch_batch_f32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream);
-int launch_batch_f64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream);
-int launch_batch_i32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream);
-int launch_batch_i64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream);
+// Batched launch over `n` entries (ogs_batch.cuh); grid <= 0 = one full wave;
+// block = 128 or 256 threads per CTA.
+int launch_batch_f32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
+                     void* stream);
+int launch_batch_f64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
+                     void* stream);
+int launch_batch_i32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
+                     void* stream);
+int launch_batch_i64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
+                     void* stream);
 
 // Device and page-locked host allocations (ogs_alloc.cpp): counted, and made
 // to fail on demand by ogs_debug_fail_alloc.  Every allocation of the library

@@ -7,7 +7,8 @@ namespace ogsgb {
 int launch_f32(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, void* stream) {
   return launch_typed<float>(m, f, mode, op, pat, stream);
 }
-int launch_batch_f32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream) {
-  return launch_batch_typed<float>(E, starts, n, nitems, grid, stream);
+int launch_batch_f32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
+                     void* stream) {
+  return launch_batch_typed<float>(E, starts, n, nitems, grid, block, stream);
 }
 }  // namespace ogsgb

@@ -7,7 +7,8 @@ namespace ogsgb {
 int launch_i32(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, void* stream) {
   return launch_typed<int32_t>(m, f, mode, op, pat, stream);
 }
-int launch_batch_i32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, void* stream) {
-  return launch_batch_typed<int32_t>(E, starts, n, nitems, grid, stream);
+int launch_batch_i32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
+                     void* stream) {
+  return launch_batch_typed<int32_t>(E, starts, n, nitems, grid, block, stream);
 }
 }  // namespace ogsgb

@@ -430,10 +430,28 @@ class ogs_batch_t:
         arr = (C.c_void_p * len(fields))(*[_ptr(x) for x in fields])
         check(lib().ogs_batch_set_fields(self._b, arr, _stream_of(stream)))
 
-    def tune(self, stream=None) -> int:
-        g = C.c_int()
-        check(lib().ogs_batch_tune(self._b, _stream_of(stream), C.byref(g)))
-        return g.value
+    def tune(self, stream=None, use_cache=True) -> dict:
+        """Run the tuner (times candidates on scratch copies of the fields,
+        or takes a cached choice); returns the configuration chosen."""
+        c = _lib.OgsBatchConfig()
+        check(lib().ogs_batch_tune_ex(self._b, _stream_of(stream), 0 if use_cache else _lib.TUNE_NO_CACHE,
+                                      C.byref(c)))
+        return self._cfg_dict(c)
+
+    @staticmethod
+    def _cfg_dict(c):
+        return {"block": c.block, "ctas_per_sm": c.ctas_per_sm, "solo_items": c.solo_items,
+                "solo_streams": c.solo_streams, "sms": c.sms, "from_cache": bool(c.from_cache), "ms": c.ms}
+
+    @property
+    def config(self) -> dict:
+        c = _lib.OgsBatchConfig()
+        check(lib().ogs_batch_get_config(self._b, C.byref(c)))
+        return self._cfg_dict(c)
+
+    def set_config(self, block=256, ctas_per_sm=0, solo_items=0, solo_streams=1, stream=None):
+        c = _lib.OgsBatchConfig(int(block), int(ctas_per_sm), int(solo_items), int(solo_streams), 0, 0, 0, 0.0)
+        check(lib().ogs_batch_set_config(self._b, C.byref(c), _stream_of(stream)))
 
     @property
     def items(self) -> int:

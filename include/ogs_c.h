@@ -300,7 +300,10 @@ ogs_status ogs_gslib_gs_many(ogs_handle h, void *const *d_us, int vn, int dom, i
  * semantics (ogsOperator.cpp:311-360) with its own op, transpose and k to its
  * own interleaved device field; the results equal one ogs_gather_scatter per
  * entry bit for bit.  All entries share one value type and device.  Entries
- * must not share a field buffer. */
+ * must not share a field buffer.  A batch call is one persistent launch over
+ * the entries below a size threshold plus, for the entries at or above it,
+ * the single-mesh kernel on parallel branches beside it (the threshold 0
+ * puts every entry in the persistent launch). */
 typedef struct ogs_batch_s *ogs_batch;
 typedef struct {
   ogs_handle h;   /* mesh */
@@ -310,16 +313,45 @@ typedef struct {
   int32_t trans;  /* ogs_transpose */
   int32_t reserved;
 } ogs_batch_entry;
+/* The choices the tuner makes (the reference hard-codes its launch shape:
+ * blockSize 256 and 512-member row blocks, include/ogs/ogsOperator.hpp:121-123). */
+typedef struct {
+  int32_t block;        /* threads per CTA of the persistent launch: 128 or 256 */
+  int32_t ctas_per_sm;  /* its CTAs per SM (0 = as many as fit) */
+  int64_t solo_items;   /* entries with at least this many work items (warp tiles x k)
+                           run alone on the single-mesh kernel (0 = none) */
+  int32_t solo_streams; /* parallel branches those launches are spread over (1..4) */
+  int32_t sms;          /* (out) SMs of the device */
+  int32_t from_cache;   /* (out) the tuner took this from its cache */
+  int32_t reserved;
+  double ms;            /* (out) the tuner's time for one batch call, ms */
+} ogs_batch_config;
 #define OGS_BATCH_GRAPH 1u  /* capture the launch in a CUDA graph on first use, replay after */
 ogs_status ogs_batch_create(ogs_batch *out, int type, const ogs_batch_entry *entries, int n, unsigned flags);
 /* Point the entries at new fields (one per entry); synchronises `stream`. */
 ogs_status ogs_batch_set_fields(ogs_batch b, void *const *d_vs, void *stream);
 /* All entries' gather-scatters, asynchronously on `stream`. */
 ogs_status ogs_batch_gather_scatter(ogs_batch b, void *stream);
-/* Time the candidate launch shapes (1..6 persistent CTAs per SM) on the
- * batch's own fields -- which they update in place -- and keep the fastest. */
+ogs_status ogs_batch_get_config(ogs_batch b, ogs_batch_config *cfg);
+/* Use this configuration (its outputs are ignored); synchronises `stream`. */
+ogs_status ogs_batch_set_config(ogs_batch b, const ogs_batch_config *cfg, void *stream);
+/* The tuner: times candidate configurations (block size x CTAs per SM of the
+ * persistent launch, then size thresholds x branches for the single-mesh
+ * launches, then CTAs per SM again) on scratch copies of the fields -- the
+ * caller's fields are read once and never written -- and keeps the fastest.
+ * The choice is cached for the process under a key of the value type, the SM
+ * count, the k range and the histogram of log2(warp tiles) over the entries;
+ * a batch with the same key takes the cached choice without timing.
+ * OGS_TUNE_NO_CACHE times anyway (and refreshes the cache). */
+#define OGS_TUNE_NO_CACHE 1u
+ogs_status ogs_batch_tune_ex(ogs_batch b, void *stream, unsigned flags, ogs_batch_config *chosen);
+/* ogs_batch_tune_ex with flags 0; *chosen_grid = the persistent launch's CTAs. */
 ogs_status ogs_batch_tune(ogs_batch b, void *stream, int *chosen_grid);
-/* Work items (warp tile x component) the batched launch walks. */
+/* The tuner's cache key for entries of records[i] warp tiles and ks[i] components. */
+ogs_status ogs_batch_tune_key(int type, int sms, int n, const int64_t *records, const int32_t *ks,
+                              uint64_t *key);
+ogs_status ogs_batch_tune_cache_clear(void);
+/* Work items (warp tile x component) of all entries. */
 ogs_status ogs_batch_items(ogs_batch b, int64_t *items);
 ogs_status ogs_batch_free(ogs_batch b);
 

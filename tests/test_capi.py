@@ -105,3 +105,26 @@ def test_python_mirror_raises(built_lib):
     g = ogs.ogs_t().Setup(4, ids.copy(), host_only=True)
     assert not g.gather_defined  # two members of group 1 are positive
     assert (g.N, g.NlocalT, g.Ngather) == (4, 3, 3)
+
+
+def test_batch_tuner_cache_key(built_lib):
+    """The tuner caches per (value type, SM count, k range, histogram of
+    log2(warp tiles) over the entries): the order of the entries and sizes
+    within one power of two do not change the key; the type, the SM count,
+    the k range and the size classes do."""
+    def key(type_, sms, recs, ks):
+        k = C.c_uint64()
+        r = np.asarray(recs, np.int64)
+        kk = np.asarray(ks, np.int32)
+        assert built_lib.ogs_batch_tune_key(type_, sms, r.size, r.ctypes.data, kk.ctypes.data, C.byref(k)) == \
+            _lib.OGS_OK
+        return k.value
+    base = key(1, 152, [10, 300, 5000], [1, 2, 4])
+    assert key(1, 152, [5000, 10, 300], [4, 1, 2]) == base      # order
+    assert key(1, 152, [11, 260, 4100], [2, 1, 4]) == base      # same powers of two, same k range
+    assert key(0, 152, [10, 300, 5000], [1, 2, 4]) != base      # type
+    assert key(1, 148, [10, 300, 5000], [1, 2, 4]) != base      # SM count
+    assert key(1, 152, [10, 300, 5000], [1, 2, 8]) != base      # k range
+    assert key(1, 152, [10, 300, 9000], [1, 2, 4]) != base      # a size class
+    assert key(1, 152, [10, 300, 5000, 5000], [1, 2, 4, 4]) != base  # how many per class
+    assert built_lib.ogs_batch_tune_key(1, 152, 2, None, None, C.byref(C.c_uint64())) == _lib.OGS_EINVAL

@@ -58,10 +58,11 @@ def test_batch_graph_tune_and_new_fields(cuda, oracle_mod):
     mix = build_mix(oracle_mod, 40, seed=11, dtype=np.float64)
     fields = [torch.from_numpy(v.copy()).cuda() for (_, _, v, _, _, _) in mix]
     b = ogs.ogs_batch_t([(g, d, k, op, trans) for (g, _, _, k, op, trans), d in zip(mix, fields)], graph=True)
-    grid = b.tune()
-    assert grid > 0
-    for d, (_, _, v, _, _, _) in zip(fields, mix):  # tuning ran on the fields
-        d.copy_(torch.from_numpy(v))
+    cfg = b.tune(use_cache=False)
+    assert cfg["block"] in (128, 256) and cfg["ctas_per_sm"] >= 1 and cfg["ms"] > 0 and not cfg["from_cache"]
+    for d, (_, _, v, _, _, _) in zip(fields, mix):  # the tuner timed on scratch copies
+        assert same_bits(d.cpu().numpy(), v)
+    assert b.tune()["from_cache"]  # the same key again
     b.GatherScatter()  # captures
     torch.cuda.synchronize()
     check(mix, fields)
@@ -87,3 +88,25 @@ def test_batch_of_one_equals_plain_call(cuda, oracle_mod):
     g.GatherScatter(c, 2, ogs.Add, ogs.Sym)
     torch.cuda.synchronize()
     assert torch.equal(a, c)
+
+
+@pytest.mark.parametrize("cfg", [dict(), dict(block=128, ctas_per_sm=3), dict(solo_items=1, solo_streams=3),
+                                 dict(solo_items=40, solo_streams=2, ctas_per_sm=1)],
+                         ids=["default", "block128", "all-solo", "mixed"])
+def test_batch_configurations_give_the_same_results(cuda, oracle_mod, cfg):
+    """Every configuration the tuner may choose -- block size, CTAs per SM,
+    entries run alone on the single-mesh kernel over parallel graph branches
+    -- gives each entry the oracle's result."""
+    mix = build_mix(oracle_mod, 30, seed=13, dtype=np.float64, signed=True, general=True)
+    fields = [torch.from_numpy(v.copy()).cuda() for (_, _, v, _, _, _) in mix]
+    b = ogs.ogs_batch_t([(g, d, k, op, trans) for (g, _, _, k, op, trans), d in zip(mix, fields)], graph=True)
+    b.set_config(**cfg)
+    got = b.config
+    for key, val in cfg.items():
+        assert got[key] == val
+    for _ in range(2):  # capture, then replay
+        for d, (_, _, v, _, _, _) in zip(fields, mix):
+            d.copy_(torch.from_numpy(v))
+        b.GatherScatter()
+        torch.cuda.synchronize()
+        check(mix, fields)
