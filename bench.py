@@ -81,6 +81,8 @@ def parse():
     ap.add_argument("--served-requests", type=int, default=100000)
     ap.add_argument("--sweep", action="store_true",
                     help="print the results tables (one JSON line per case) instead of the bench line")
+    ap.add_argument("--cases", default=None, metavar="REGEX",
+                    help="with --sweep: only the cases whose name matches")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     if a.many and a.mode != "gs":
@@ -905,6 +907,12 @@ def run_sweep(a):
         cut = len(ts) // 10
         return float(ts[cut:len(ts) - cut].mean())
 
+    import re
+    pick = re.compile(a.cases) if a.cases else None
+
+    def wanted(case):
+        return pick is None or pick.search(case) is not None
+
     def emit(case, g, k, t, ab, warm=None):
         r = {"case": case, "local_dofs": int(g.N), "global_dofs": int(g.NgatherGlobal), "k": k,
              "us_cold": t * 1e6, "dofs_per_s_cold": g.NgatherGlobal * k / t, "gbs_cold": ab / t / 1e9,
@@ -914,6 +922,8 @@ def run_sweep(a):
         print(json.dumps(r), flush=True)
 
     def gs(case, g, x, k, op, ab, many=None):
+        if not wanted(case):
+            return
         if many is None:
             x0 = x.clone()
             fn = lambda: L.ogs_gather_scatter(g.handle, x.data_ptr(), k, tcode[x.dtype], op, 0, st.cuda_stream)
@@ -939,7 +949,17 @@ def run_sweep(a):
     def idx_bytes(g):
         return 4 * g.nnzT + 4 * (g.NlocalT + 1)
 
+    # the floor of this harness: a one-element fill kernel between the same
+    # events, after the same L2 flush
+    one = torch.zeros(1, dtype=torch.float32, device=dev)
+    t_empty = timeit(lambda: (one.fill_(1.0), 0)[1])
+    print(json.dumps({"case": "empty launch (one-element fill kernel)", "us_cold": t_empty * 1e6}), flush=True)
+
     for p in range(1, 16):
+        if pick is not None and not any(wanted(f"24^3 p={p} {c}") for c in
+                                        ("f64 Add GS", "f32 Add GS", "int32 Min GS", "int32 Max GS", "int64 Min GS",
+                                         "int64 Max GS", "f64 Gather Trans", "f64 Scatter NoTrans")):
+            continue
         ids = mesh.box_ids(24, 24, 24, p)
         g = ogs.ogs_t().Setup(ids.size, ids.copy())
         x = torch.from_numpy(mesh.uniform_values(ids.size, np.float64, -1, 1, p)).to(dev)
@@ -965,7 +985,8 @@ def run_sweep(a):
                                                                  st.cuda_stream)),
                            ("Scatter NoTrans", lambda: L.ogs_scatter(sg.handle, x.data_ptr(), gv.data_ptr(), 1, 1, 1,
                                                                      st.cuda_stream))):
-                emit(f"24^3 p=7 f64 {nm}", sg, 1, timeit(fn), abg, timeit(fn, cold=False))
+                if wanted(f"24^3 p=7 f64 {nm}"):
+                    emit(f"24^3 p=7 f64 {nm}", sg, 1, timeit(fn), abg, timeit(fn, cold=False))
             del sg, gv
         del g, x
     ids = mesh.permute_elements(mesh.box_ids(32, 32, 16, 5), 5, seed=2024)

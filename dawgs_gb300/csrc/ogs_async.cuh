@@ -16,10 +16,6 @@
 //                          wait for the gathers of item i (stage s)
 //                          fold item i from shared memory, store
 //
-// With k > 1 components, a warp runs the k components of a tile one after
-// another as consecutive items, so the tile's column ids are loaded once and
-// carried from item to item.
-//
 // Every lane gathers and later folds its own entries only, so no barrier of
 // any kind is needed: cp.async.wait_group makes a thread's own completed
 // copies visible to it.  Two stages suffice: the stage an iteration refills
@@ -38,6 +34,10 @@
 #endif
 
 namespace ogsgb {
+
+#ifndef OGS_WARP_MAJOR
+#define OGS_WARP_MAJOR 0
+#endif
 
 #ifndef OGS_ASYNC_STAGES
 #define OGS_ASYNC_STAGES 2
@@ -118,50 +118,51 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
   const int K = KL == kK1 ? 1 : f.K;
   const int64_t nw = m.nwtiles;
   const int64_t nitems = nw * K;
-  const int64_t wid = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + warp;
-  // k = 1: warp w takes items w, w+W, ... (the grid sweeps the mesh front to
-  // back).  k > 1: items are (tile, component) pairs, tile-major, and warp w
-  // takes a contiguous run of them, balanced to one item: the k components
-  // of a tile follow one another in one warp, which loads the tile's
-  // descriptor and column ids once for all of them.  Items are followed as
-  // (tile, component) pairs, advanced without division.
-  int64_t i, step, iend;
-  int tcur, ccur;
-  if (KL == kK1) {
-    i = wid;
-    step = W;
-    iend = nitems;
-    tcur = static_cast<int>(i);
-    ccur = 0;
-  } else {
-    const int64_t q = nitems / W, r = nitems % W;
-    i = wid * q + (wid < r ? wid : r);
-    step = 1;
-    iend = i + q + (wid < r ? 1 : 0);
-    tcur = static_cast<int>(i / K);
-    ccur = static_cast<int>(i - static_cast<int64_t>(tcur) * K);
-  }
-  if (i >= iend) return;
+  // warp-major numbering (OGS_WARP_MAJOR): consecutive items go to the same
+  // warp slot of consecutive CTAs, so neighbouring tiles run on different SMs
+  // and the warps holding one item more than the others are spread evenly
+  // over the CTAs
+  const int64_t wid = OGS_WARP_MAJOR ? static_cast<int64_t>(warp) * gridDim.x + blockIdx.x
+                                     : static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + warp;
+  // Warp w takes items w, w+W, w+2W, ...: the grid sweeps the mesh front to
+  // back.  k > 1 interleaved: item = (tile, component), tile-major, so the k
+  // warps of one tile run side by side and share the sectors of each node's
+  // k values; separate arrays: item = (array, tile), array-major, so one
+  // array and the column ids stay in L2 while the grid sweeps it.  (A warp
+  // running a contiguous run of (tile, component) items, loading each tile's
+  // column ids once, was measured much slower: 83 vs 62 us for k = 3 on 3.5 M
+  // permuted nodes.)  Items are followed as (tile, component) pairs, advanced
+  // by W without division.
+  const int64_t i0 = wid;
+  if (i0 >= nitems) return;
+  int64_t i = i0;
+  const int64_t step = W, iend = nitems;
+  // item = outer * M + inner; interleaved: (tile, comp), M = K; many: (comp, tile), M = nw
+  const int M = KL == kKMany ? static_cast<int>(nw) : (KL == kKInterleaved ? K : 1);
+  const int Wi = static_cast<int>(W);
+  const int Wq = KL == kK1 ? Wi : Wi / M, Wr = KL == kK1 ? 0 : Wi % M;
+  const int o0 = KL == kK1 ? static_cast<int>(i0) : static_cast<int>(i0 / M);
+  const int n0 = KL == kK1 ? 0 : static_cast<int>(i0 - static_cast<int64_t>(o0) * M);
+  int tcur = KL == kKMany ? n0 : o0;
+  int ccur = KL == kKMany ? o0 : n0;
   const bool use_mask = !PLAIN && (pat.gather_n || pat.scatter_n) && m.signed_maps;
   const bool gmask = !PLAIN && pat.gather_n != 0;
   const int smode = PLAIN ? 0 : pat.scatter_n;
   const bool gslib = !PLAIN && pat.gslib != 0;
   const int64_t stride = KL == kKInterleaved ? K : 1;
-  const int Wi = static_cast<int>(W);
-  // the item after (t, c); `same` tells whether it is another component of tile t
-  auto advance = [&](int t, int c, int& tn, int& cn, bool& same) {
+  // the item W after (t, c)
+  auto advance = [&](int t, int c, int& tn, int& cn) {
     if (KL == kK1) {
       tn = t + Wi;
       cn = 0;
-      same = false;
-    } else if (c + 1 < K) {
-      tn = t;
-      cn = c + 1;
-      same = true;
+    } else if (KL == kKInterleaved) {
+      cn = c + Wr;
+      tn = t + Wq;
+      if (cn >= M) { cn -= M; tn += 1; }
     } else {
-      tn = t + 1;
-      cn = 0;
-      same = false;
+      tn = t + Wr;
+      cn = c + Wq;
+      if (tn >= M) { tn -= M; cn += 1; }
     }
   };
   T* gv = static_cast<T*>(f.gv);
@@ -170,16 +171,15 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
   // trip, the column ids of the first two in the next, then the gathers of
   // item i; the loop's first pass issues the gathers of the next item at once
   int tnxt = 0, cnxt = 0, tnn = 0, cnn = 0;
-  bool snxt_same = false, snn_same = false;
   const bool has1 = i + step < iend;
   Tile cur = m.wtiles[tcur];
   Tile nxt{}, nn{};
   if (has1) {
-    advance(tcur, ccur, tnxt, cnxt, snxt_same);
-    nxt = snxt_same ? cur : m.wtiles[tnxt];
+    advance(tcur, ccur, tnxt, cnxt);
+    nxt = m.wtiles[tnxt];
     if (i + 2 * step < iend) {
-      advance(tnxt, cnxt, tnn, cnn, snn_same);
-      nn = snn_same ? nxt : m.wtiles[tnn];
+      advance(tnxt, cnxt, tnn, cnn);
+      nn = m.wtiles[tnn];
     }
   }
   WarpState scur, snxt;
@@ -188,13 +188,9 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
   OGS_DEGREE_SWITCH(cur.bucket, OGS_A_LOAD_CUR)
 #undef OGS_A_LOAD_CUR
   if (has1) {
-    if (snxt_same) {
-      snxt = scur;
-    } else {
 #define OGS_A_LOAD_NXT(D) OGS_A_LOAD(D, nxt, tnxt, snxt)
-      OGS_DEGREE_SWITCH(nxt.bucket, OGS_A_LOAD_NXT)
+    OGS_DEGREE_SWITCH(nxt.bucket, OGS_A_LOAD_NXT)
 #undef OGS_A_LOAD_NXT
-    }
   }
   {
     const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, ccur);
@@ -220,18 +216,13 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
     WarpState snn;
     Tile n3{};
     int tn3 = 0, cn3 = 0;
-    bool sn3_same = false;
     if (more2) {
-      if (snn_same) {
-        snn = snxt;  // another component of the same tile: its column ids are loaded
-      } else {
 #define OGS_A_LOAD_NN(D) OGS_A_LOAD(D, nn, tnn, snn)
-        OGS_DEGREE_SWITCH(nn.bucket, OGS_A_LOAD_NN)
+      OGS_DEGREE_SWITCH(nn.bucket, OGS_A_LOAD_NN)
 #undef OGS_A_LOAD_NN
-      }
       if (i + 3 * step < iend) {
-        advance(tnn, cnn, tn3, cn3, sn3_same);
-        n3 = sn3_same ? nn : m.wtiles[tn3];
+        advance(tnn, cnn, tn3, cn3);
+        n3 = m.wtiles[tn3];
       }
     }
     cp_async_wait<1>();  // the gathers of item i are in
@@ -261,10 +252,70 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
     nn = n3;
     tnn = tn3;
     cnn = cn3;
-    snn_same = sn3_same;
   }
   cp_async_wait<0>();
 #undef OGS_A_LOAD
+}
+
+// Small meshes: when every warp tile fits in about one wave of warps, the
+// persistent pipeline has nothing to overlap and its three dependent round
+// trips (descriptor, column ids, values) are paid in full.  This kernel
+// gives each warp one tile and finds it without a descriptor load: tiles are
+// counted bucket by bucket from the bucket sizes in the kernel parameters
+// (all tiles run at once, so their order does not matter).  Column ids, then
+// values, then the fold: two round trips.  GatherScatter, k = 1, every member
+// taking part (the plain pattern); the fold and the stores are those of the
+// warp pipeline (ogsOperator.cpp:311-360).
+#ifndef OGS_WAVE_FACTOR
+#define OGS_WAVE_FACTOR 0
+#endif
+#ifndef OGS_WAVE_MINB
+#define OGS_WAVE_MINB 4
+#endif
+
+template <typename T, int OP>
+__global__ void __launch_bounds__(kBlock, OGS_WAVE_MINB) ogs_wave_kernel(const DevMaps m, const FieldArgs f) {
+  const int lane = static_cast<int>(threadIdx.x) & 31;
+  int t = static_cast<int>(blockIdx.x) * (kBlock / 32) + (static_cast<int>(threadIdx.x) >> 5);
+  int d = 1;
+  for (; d <= kDmax; ++d) {
+    const int per = warp_rows_per_tile(d);
+    const int tn = (m.b[d].n + per - 1) / per;
+    if (t < tn) break;
+    t -= tn;
+  }
+  if (d > kDmax) return;
+  T* v = static_cast<T*>(f.v);
+  const Pattern pat{0, 0, 0, 0};
+#define OGS_W_RUN(D)                                                                       \
+  do {                                                                                     \
+    Tile tile;                                                                             \
+    tile.bucket = D;                                                                       \
+    tile.begin = t * warp_rows_per_tile(D);                                                \
+    tile.count = min(warp_rows_per_tile(D), m.b[D].n - tile.begin);                         \
+    tile.first_row = 0;                                                                    \
+    WarpState s;                                                                           \
+    warp_load_state<kModeGS, D>(m.b[D], tile, nullptr, 0, false, pat, lane, s);          \
+    T V[kWarpSlots];                                                                       \
+    warp_load_vals<T, kModeGS, D>(s, v, nullptr, 1, 1, 0, false, lane, V);                 \
+    warp_fold_store<T, OP, kModeGS, D>(s, v, nullptr, 1, 1, 0, false, 0, false, lane, V); \
+  } while (0)
+  OGS_DEGREE_SWITCH(d, OGS_W_RUN)
+#undef OGS_W_RUN
+}
+
+// Warps of the one-wave kernel resident at once on the device.
+template <typename T, int OP>
+inline int64_t wave_capacity() {
+  static DeviceCache cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return cache.get(dev, [dev] {
+    int bps = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_wave_kernel<T, OP>, kBlock, 0);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1) * (kBlock / 32);
+  });
 }
 
 template <typename T, int OP, int MODE, int KL, bool PLAIN>
@@ -290,7 +341,20 @@ inline int async_grid(int64_t nitems) {
 template <typename T, int OP, int MODE, int KL>
 inline void launch_async_kl(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
   const int64_t nitems = static_cast<int64_t>(m.nwtiles) * (KL == kK1 ? 1 : f.K);
-  if (!pat.gather_n && !pat.scatter_n && !pat.limit_n && !pat.gslib) {
+  const bool plain = !pat.gather_n && !pat.scatter_n && !pat.limit_n && !pat.gslib;
+  if constexpr (KL == kK1 && MODE == kModeGS) {
+    // the one-wave kernel derives tiles from the bucket sizes: only for the
+    // whole map (not a slice of its tiles, as the host-buffer pipeline runs)
+    int64_t all_tiles = 0;
+    for (int d = 1; d <= kDmax; ++d) all_tiles += (m.b[d].n + warp_rows_per_tile(d) - 1) / warp_rows_per_tile(d);
+    if (OGS_WAVE_FACTOR > 0 && plain && all_tiles == m.nwtiles &&
+        nitems <= static_cast<int64_t>(OGS_WAVE_FACTOR * static_cast<double>(wave_capacity<T, OP>()))) {
+      const int grid = static_cast<int>((nitems + (kBlock / 32) - 1) / (kBlock / 32));
+      ogs_wave_kernel<T, OP><<<grid, kBlock, 0, s>>>(m, f);
+      return;
+    }
+  }
+  if (plain) {
     const int grid = async_grid<T, OP, MODE, KL, true>(nitems);
     ogs_async_kernel<T, OP, MODE, KL, true><<<grid, kBlock, async_smem_bytes<T>(), s>>>(m, f, pat);
   } else {

@@ -4,11 +4,10 @@
 // handle carries, from setup, one 32-byte record per warp tile (WarpRec:
 // column and row arrays of its bucket, first row, degree and row count); the
 // batch adds a prefix table `starts` over the entries' (record, component)
-// items.  Warp w of the grid takes a contiguous run of items, so a record's k
-// components follow one another in one warp (its column ids are loaded once)
-// and the walk from item to item needs no search, and runs the same per-warp
-// pipeline as ogs_warp.cuh: the next item's column ids load while the
-// current item's values are gathered, folded and stored.  The fold follows
+// items.  Warp w of the grid takes items w, w+W, ..., finds an item's entry
+// by binary search (in shared memory for up to kBatchSmem entries), and runs
+// the same per-warp pipeline as ogs_warp.cuh: the next item's column ids load
+// while the current item's values are gathered, folded and stored.  The fold follows
 // ogsOperator.cpp:311-360 with the entry's op chosen at run time
 // (warp-uniform), so one launch serves entries with different ops.
 #pragma once
@@ -76,7 +75,8 @@ __device__ __forceinline__ void batch_load_rec(BatchItem& it) {
   it.nP = w.nP;
 }
 
-// The item at global index i (one binary search; once per warp).
+// The item at global index i: its entry by binary search over the prefix,
+// then its record and component.
 __device__ __forceinline__ void batch_item_at(const BatchEntry* E, const int64_t* st, int n, int64_t i,
                                               BatchItem& it) {
   batch_load_entry(E, batch_entry_of(st, n, i), it);
@@ -84,30 +84,6 @@ __device__ __forceinline__ void batch_item_at(const BatchEntry* E, const int64_t
   it.r = static_cast<int32_t>(local / it.K);
   it.k = static_cast<int32_t>(local - static_cast<int64_t>(it.r) * it.K);
   batch_load_rec(it);
-}
-
-// The item after `a` (global index i_next = a's index + 1): the next
-// component of the same record, the next record, or the first record of the
-// next entry with any.  Returns whether it is the same record.
-__device__ __forceinline__ bool batch_advance(const BatchEntry* E, const int64_t* st, int n, int64_t i_next,
-                                              const BatchItem& a, BatchItem& b) {
-  b = a;
-  if (i_next < st[a.e + 1]) {
-    if (a.k + 1 < a.K) {
-      b.k = a.k + 1;
-      return true;
-    }
-    b.r = a.r + 1;
-    b.k = 0;
-  } else {
-    int e = a.e + 1;
-    while (e < n - 1 && st[e + 1] == st[e]) ++e;  // entries without records
-    batch_load_entry(E, e, b);
-    b.r = 0;
-    b.k = 0;
-  }
-  batch_load_rec(b);
-  return false;
 }
 
 __device__ __forceinline__ void batch_load_state(const BatchItem& it, int lane, WarpState& s) {
@@ -132,11 +108,12 @@ __device__ __forceinline__ void batch_load_state(const BatchItem& it, int lane, 
 #undef OGS_B_LOAD
 }
 
-// Warp w takes a contiguous run of the (entry, record, component) items,
-// balanced to one item: the k components of a record follow one another in
-// one warp, which loads the record's column ids once for all of them, and the
-// walk from item to item needs no search.  The prefix `starts` is staged in
-// shared memory (dynamic, (n+1) entries) when it fits.
+// Warp w takes items w, w+W, ... of the (entry, record, component) items, so
+// the grid sweeps every mesh front to back and the k components of a record
+// run on neighbouring warps at once, sharing its column ids and the field's
+// sectors through L1/L2 (a warp walking a contiguous run of items was much
+// slower on large meshes, as for the single-mesh kernel).  The prefix
+// `starts` is staged in shared memory (dynamic, (n+1) entries) when it fits.
 template <typename T, int BLOCK>
 __global__ void __launch_bounds__(BLOCK, OGS_BATCH_MINB * 256 / BLOCK)
     ogs_batch_kernel(const BatchEntry* __restrict__ E, const int64_t* __restrict__ starts, int n) {
@@ -149,21 +126,17 @@ __global__ void __launch_bounds__(BLOCK, OGS_BATCH_MINB * 256 / BLOCK)
   const int64_t nitems = st[n];
   const int lane = static_cast<int>(threadIdx.x) & 31;
   const int64_t W = static_cast<int64_t>(gridDim.x) * (BLOCK / 32);
-  const int64_t wid = static_cast<int64_t>(blockIdx.x) * (BLOCK / 32) + (threadIdx.x >> 5);
-  const int64_t q = nitems / W, rem = nitems % W;
-  int64_t i = wid * q + (wid < rem ? wid : rem);
-  const int64_t iend = i + q + (wid < rem ? 1 : 0);
-  if (i >= iend) return;
+  int64_t i = static_cast<int64_t>(blockIdx.x) * (BLOCK / 32) + (threadIdx.x >> 5);
+  if (i >= nitems) return;
 
   BatchItem cur, nxt;
   batch_item_at(E, st, n, i, cur);
   WarpState scur;
   batch_load_state(cur, lane, scur);
-  bool nxt_same = false;
-  if (i + 1 < iend) nxt_same = batch_advance(E, st, n, i + 1, cur, nxt);
+  if (i + W < nitems) batch_item_at(E, st, n, i + W, nxt);
 
   for (;;) {
-    const bool more = i + 1 < iend;
+    const bool more = i + W < nitems;
     const int K = cur.K, k = cur.k, d = cur.bucket_count >> 16;
     const bool gmask = (cur.flags >> 4) & 1;
     const int smode = (cur.flags >> 5) & 1;
@@ -174,21 +147,18 @@ __global__ void __launch_bounds__(BLOCK, OGS_BATCH_MINB * 256 / BLOCK)
 #undef OGS_B_VALS
     WarpState snxt;
     BatchItem nn;
-    bool nn_same = false;
     if (more) {
-      if (nxt_same) snxt = scur;  // another component of the same record
-      else batch_load_state(nxt, lane, snxt);
-      if (i + 2 < iend) nn_same = batch_advance(E, st, n, i + 2, nxt, nn);
+      batch_load_state(nxt, lane, snxt);
+      if (i + 2 * W < nitems) batch_item_at(E, st, n, i + 2 * W, nn);
     }
 #define OGS_B_FOLD(D) fold_store_rt<T, D>(cur.flags & 15, scur, base, K, K, k, gmask, smode, lane, V)
     OGS_DEGREE_SWITCH(d, OGS_B_FOLD)
 #undef OGS_B_FOLD
     if (!more) break;
-    i += 1;
+    i += W;
     cur = nxt;
     scur = snxt;
     nxt = nn;
-    nxt_same = nn_same;
   }
 }
 

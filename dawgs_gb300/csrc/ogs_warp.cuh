@@ -163,10 +163,9 @@ enum KLayout : int {
                       // the sectors of each node's k values.  (One item per
                       // tile looping over the components was slower: 86 vs
                       // 66 us for k = 3 on 3.5 M permuted nodes.)
-  kKMany = 2,       // k separate arrays: item = (array, tile), array-major in
-                    // this kernel (one array and the column ids stay in L2
-                    // while the grid sweeps it); ogs_async_kernel runs
-                    // (tile, array) pairs tile-major, a warp a contiguous run
+  kKMany = 2,       // k separate arrays: item = (array, tile), array-major, so
+                    // one array and the column ids stay resident in L2 while
+                    // the grid sweeps that array
 };
 
 template <typename T, int OP, int MODE, int KL>

@@ -59,7 +59,8 @@ def test_setup_frees_everything_on_allocation_failure(cuda, flags):
 def test_reserve_host_then_host_calls_allocate_nothing(cuda, oracle_mod):
     L = _lib.lib()
     ids = mesh.box_ids(8, 8, 8, 3)
-    g = ogs.ogs_t().Setup(ids.size, ids.copy())
+    sids = ids.copy()
+    g = ogs.ogs_t().Setup(sids.size, sids, None, ogs.Signed, ogs.Auto, True)  # Gather is well defined
     h = g.handle
     stream = None
     # a failed reservation returns OGS_ENOMEM and frees what it took
@@ -67,7 +68,7 @@ def test_reserve_host_then_host_calls_allocate_nothing(cuda, oracle_mod):
     assert n >= 1
     assert L.ogs_reserve_host(h, 3, 1) == _lib.OGS_OK
     before = held(L)
-    ref = oracle_mod.OracleOgs(ids.copy(), "unsigned")
+    ref = oracle_mod.OracleOgs(ids.copy(), "signed", unique=True)
     # with the next allocation armed to fail, every _host call no larger than
     # the reservation succeeds: none of them allocates
     L.ogs_debug_fail_alloc(1)
