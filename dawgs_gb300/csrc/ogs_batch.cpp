@@ -4,7 +4,7 @@
 //
 // A batch runs as one CUDA graph: the entries below a size threshold go to one
 // persistent launch of the batched kernel (ogs_batch.cuh, the register
-// pipeline; a warp walks contiguous (entry, record, component) items), and
+// pipeline over the entries' (record, component) items), and
 // the entries at or above it each run the single-mesh kernel (ogs_async.cuh,
 // the cp.async ring) on their own launch, spread over parallel branches of
 // the graph so that they run beside the persistent launch.  The tuner chooses
@@ -49,7 +49,7 @@ struct ogs_batch_s {
 namespace ogsgb {
 namespace {
 
-constexpr int kMaxBranches = 4;
+constexpr int kMaxBranches = 8;
 
 ogs_status cuda_err(cudaError_t e, const char* fn, const char* what) {
   if (e == cudaSuccess) return OGS_OK;
@@ -353,7 +353,7 @@ ogs_status ogs_batch_set_config(ogs_batch b, const ogs_batch_config* cfg, void* 
   if ((cfg->block != 128 && cfg->block != 256) || cfg->ctas_per_sm < 0 || cfg->solo_items < 0 ||
       cfg->solo_streams < 1 || cfg->solo_streams > kMaxBranches)
     return set_error(OGS_EINVAL, "ogs_batch_set_config: block 128 or 256, ctas_per_sm >= 0, solo_items >= 0, "
-                                 "1 <= solo_streams <= 4");
+                                 "1 <= solo_streams <= 8");
   ogs_status s = ensure_branches(b, cfg->solo_streams, fn);
   if (s != OGS_OK) return s;
   const int sms = b->cfg.sms;
@@ -455,12 +455,13 @@ ogs_status ogs_batch_tune_ex(ogs_batch b, void* stream, unsigned flags, ogs_batc
       cand.solo_streams = 1;
       s = consider(cand);
     }
-  // 2) entries from a size on run alone on the single-mesh kernel, over 1..4
-  // branches: thresholds at 1/4, 1, 4 and 16 waves of warps of the persistent grid
+  // 2) entries from a size on run alone on the single-mesh kernel, over 2, 4
+  // or 8 branches: thresholds at 1/16, 1/4, 1 and 4 waves of warps of the
+  // persistent grid
   const int64_t wave = static_cast<int64_t>(saved.sms) * 24;
   const ogs_batch_config base = best;
-  for (int64_t t : {wave / 4, wave, 4 * wave, 16 * wave})
-    for (int nb : {1, 2, 4}) {
+  for (int64_t t : {wave / 16, wave / 4, wave, 4 * wave})
+    for (int nb : {2, 4, 8}) {
       if (s != OGS_OK) break;
       bool any = false;
       for (int64_t it : b->items) any = any || it >= t;

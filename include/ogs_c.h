@@ -320,7 +320,7 @@ typedef struct {
   int32_t ctas_per_sm;  /* its CTAs per SM (0 = as many as fit) */
   int64_t solo_items;   /* entries with at least this many work items (warp tiles x k)
                            run alone on the single-mesh kernel (0 = none) */
-  int32_t solo_streams; /* parallel branches those launches are spread over (1..4) */
+  int32_t solo_streams; /* parallel branches those launches are spread over (1..8) */
   int32_t sms;          /* (out) SMs of the device */
   int32_t from_cache;   /* (out) the tuner took this from its cache */
   int32_t reserved;
