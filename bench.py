@@ -171,8 +171,9 @@ class Clocks:
         out["timed_region_ms"] = 1e3 * (self._m1 - self._m0)
         out["sample_period_ms"] = 50
         if whole is not None:
-            # every GPU leg of this run (cold and warm kernel loops, e2e, the
-            # baselines): the region above is too short for many 50 ms samples
+            # the kernel legs of this run (cold and warm loops, the reference
+            # device algorithm, e2e): the region above is too short for many
+            # 50 ms samples
             out["whole_run"] = whole
         return out
 
@@ -383,13 +384,13 @@ def run_served(a, dev, L, stream):
     later request finds what earlier ones left there (after many repeated Adds
     that includes +-inf and NaN bit patterns): this leg measures throughput and
     latency, the per-request results are checked by the served tests.
-    Requests are admitted against a 16 GB device budget.  First a saturation run (all requests queued at once) gives the
-    throughput; then Poisson arrivals at 25%, 50% and 80% of it give p50/p99
-    (the whole arrival schedule is handed to the server at once, which admits
-    each request at its arrival time, so the client's own submission cost does
-    not stand in for the server's)
-    latency, counted from each request's scheduled arrival.  Plain = the same
-    requests one after another through ogs_gather_scatter_host."""
+    Requests are admitted against a 16 GB device budget.  First a saturation
+    run (all requests queued at once) gives the throughput; then Poisson
+    arrivals at 25%, 50% and 80% of it give p50/p99 latency, counted from each
+    request's scheduled arrival.  The whole arrival schedule is handed to the
+    server at once, which admits each request at its arrival time, so the
+    client's own submission cost does not stand in for the server's.  Plain =
+    the same requests one after another through ogs_gather_scatter_host."""
     import torch
     from dawgs_gb300 import mesh, ogs
     mix = mesh.mesh_mix(64, seed=77, lo=2, hi=16, pmax=7)
@@ -657,8 +658,9 @@ def run_ours(a):
         flush.zero_()
         torch.sum(flush, dim=0, out=sink)
 
-    # clocks are sampled over every GPU leg of the run; the cold timed loop
-    # is marked inside that window
+    # clocks are sampled over the kernel legs of the run (cold, warm, the
+    # reference device algorithm, e2e); the cold timed loop is marked inside
+    # that window
     clk = Clocks(local).__enter__()
     for _ in range(a.warmup):
         work.copy_(pristine)
@@ -770,6 +772,10 @@ def run_ours(a):
     work.copy_(pristine)
     step()
     torch.cuda.synchronize(dev)
+    # the sampler stops before the batched and served legs: its queries of the
+    # driver every 50 ms stall the served requests' copies and launches now
+    # and then, which would show in their latency tail
+    clk.__exit__(None, None, None)
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:
@@ -814,7 +820,6 @@ def run_ours(a):
     if rank == 0 and world == 1 and not a.no_partitioned and headline_kind:
         partitioned = run_partitioned(a, dev, stream, per_step)
 
-    clk.__exit__(None, None, None)
     peak, peak_src = hbm_peak()
     nbytes_alg = alg_bytes(ids.size, g.nnzT, g.NlocalT, a.k, s, a.mode, g.Ngather)
     achieved = nbytes_alg / per_step / 1e9

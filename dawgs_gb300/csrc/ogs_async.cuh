@@ -35,10 +35,6 @@
 
 namespace ogsgb {
 
-#ifndef OGS_WARP_MAJOR
-#define OGS_WARP_MAJOR 0
-#endif
-
 #ifndef OGS_ASYNC_STAGES
 #define OGS_ASYNC_STAGES 2
 #endif
@@ -118,12 +114,7 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
   const int K = KL == kK1 ? 1 : f.K;
   const int64_t nw = m.nwtiles;
   const int64_t nitems = nw * K;
-  // warp-major numbering (OGS_WARP_MAJOR): consecutive items go to the same
-  // warp slot of consecutive CTAs, so neighbouring tiles run on different SMs
-  // and the warps holding one item more than the others are spread evenly
-  // over the CTAs
-  const int64_t wid = OGS_WARP_MAJOR ? static_cast<int64_t>(warp) * gridDim.x + blockIdx.x
-                                     : static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + warp;
+  const int64_t wid = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + warp;
   // Warp w takes items w, w+W, w+2W, ...: the grid sweeps the mesh front to
   // back.  k > 1 interleaved: item = (tile, component), tile-major, so the k
   // warps of one tile run side by side and share the sectors of each node's
@@ -257,67 +248,6 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
 #undef OGS_A_LOAD
 }
 
-// Small meshes: when every warp tile fits in about one wave of warps, the
-// persistent pipeline has nothing to overlap and its three dependent round
-// trips (descriptor, column ids, values) are paid in full.  This kernel
-// gives each warp one tile and finds it without a descriptor load: tiles are
-// counted bucket by bucket from the bucket sizes in the kernel parameters
-// (all tiles run at once, so their order does not matter).  Column ids, then
-// values, then the fold: two round trips.  GatherScatter, k = 1, every member
-// taking part (the plain pattern); the fold and the stores are those of the
-// warp pipeline (ogsOperator.cpp:311-360).
-#ifndef OGS_WAVE_FACTOR
-#define OGS_WAVE_FACTOR 0
-#endif
-#ifndef OGS_WAVE_MINB
-#define OGS_WAVE_MINB 4
-#endif
-
-template <typename T, int OP>
-__global__ void __launch_bounds__(kBlock, OGS_WAVE_MINB) ogs_wave_kernel(const DevMaps m, const FieldArgs f) {
-  const int lane = static_cast<int>(threadIdx.x) & 31;
-  int t = static_cast<int>(blockIdx.x) * (kBlock / 32) + (static_cast<int>(threadIdx.x) >> 5);
-  int d = 1;
-  for (; d <= kDmax; ++d) {
-    const int per = warp_rows_per_tile(d);
-    const int tn = (m.b[d].n + per - 1) / per;
-    if (t < tn) break;
-    t -= tn;
-  }
-  if (d > kDmax) return;
-  T* v = static_cast<T*>(f.v);
-  const Pattern pat{0, 0, 0, 0};
-#define OGS_W_RUN(D)                                                                       \
-  do {                                                                                     \
-    Tile tile;                                                                             \
-    tile.bucket = D;                                                                       \
-    tile.begin = t * warp_rows_per_tile(D);                                                \
-    tile.count = min(warp_rows_per_tile(D), m.b[D].n - tile.begin);                         \
-    tile.first_row = 0;                                                                    \
-    WarpState s;                                                                           \
-    warp_load_state<kModeGS, D>(m.b[D], tile, nullptr, 0, false, pat, lane, s);          \
-    T V[kWarpSlots];                                                                       \
-    warp_load_vals<T, kModeGS, D>(s, v, nullptr, 1, 1, 0, false, lane, V);                 \
-    warp_fold_store<T, OP, kModeGS, D>(s, v, nullptr, 1, 1, 0, false, 0, false, lane, V); \
-  } while (0)
-  OGS_DEGREE_SWITCH(d, OGS_W_RUN)
-#undef OGS_W_RUN
-}
-
-// Warps of the one-wave kernel resident at once on the device.
-template <typename T, int OP>
-inline int64_t wave_capacity() {
-  static DeviceCache cache;
-  int dev = 0;
-  cudaGetDevice(&dev);
-  return cache.get(dev, [dev] {
-    int bps = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_wave_kernel<T, OP>, kBlock, 0);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1) * (kBlock / 32);
-  });
-}
-
 template <typename T, int OP, int MODE, int KL, bool PLAIN>
 inline int async_grid(int64_t nitems) {
   static DeviceCache cache;
@@ -342,18 +272,6 @@ template <typename T, int OP, int MODE, int KL>
 inline void launch_async_kl(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
   const int64_t nitems = static_cast<int64_t>(m.nwtiles) * (KL == kK1 ? 1 : f.K);
   const bool plain = !pat.gather_n && !pat.scatter_n && !pat.limit_n && !pat.gslib;
-  if constexpr (KL == kK1 && MODE == kModeGS) {
-    // the one-wave kernel derives tiles from the bucket sizes: only for the
-    // whole map (not a slice of its tiles, as the host-buffer pipeline runs)
-    int64_t all_tiles = 0;
-    for (int d = 1; d <= kDmax; ++d) all_tiles += (m.b[d].n + warp_rows_per_tile(d) - 1) / warp_rows_per_tile(d);
-    if (OGS_WAVE_FACTOR > 0 && plain && all_tiles == m.nwtiles &&
-        nitems <= static_cast<int64_t>(OGS_WAVE_FACTOR * static_cast<double>(wave_capacity<T, OP>()))) {
-      const int grid = static_cast<int>((nitems + (kBlock / 32) - 1) / (kBlock / 32));
-      ogs_wave_kernel<T, OP><<<grid, kBlock, 0, s>>>(m, f);
-      return;
-    }
-  }
   if (plain) {
     const int grid = async_grid<T, OP, MODE, KL, true>(nitems);
     ogs_async_kernel<T, OP, MODE, KL, true><<<grid, kBlock, async_smem_bytes<T>(), s>>>(m, f, pat);

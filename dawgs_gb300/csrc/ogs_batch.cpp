@@ -158,10 +158,10 @@ int launch_all(ogs_batch_s* b, const BatchEntry* fields, cudaStream_t st) {
     const int64_t nitems = b->starts.back();
     const int grid = b->cfg.ctas_per_sm > 0 ? b->cfg.ctas_per_sm * std::max(1, b->cfg.sms) : 0;
     switch (b->type) {
-      case OGS_FLOAT: e = launch_batch_f32(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, st); break;
-      case OGS_DOUBLE: e = launch_batch_f64(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, st); break;
-      case OGS_INT32: e = launch_batch_i32(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, st); break;
-      default: e = launch_batch_i64(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, st); break;
+      case OGS_FLOAT: e = launch_batch_f32(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy, st); break;
+      case OGS_DOUBLE: e = launch_batch_f64(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy, st); break;
+      case OGS_INT32: e = launch_batch_i32(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy, st); break;
+      default: e = launch_batch_i64(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy, st); break;
     }
     for (size_t q = 0; !e && q < b->general.size(); ++q) {
       const int i = b->general[q];
@@ -268,6 +268,7 @@ ogs_status ogs_batch_create(ogs_batch* out, int type, const ogs_batch_entry* ent
   int sms = 1;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   b->cfg.block = 256;
+  b->cfg.occupancy = 2;
   b->cfg.ctas_per_sm = 0;
   b->cfg.solo_items = 0;
   b->cfg.solo_streams = 1;
@@ -351,14 +352,16 @@ ogs_status ogs_batch_set_config(ogs_batch b, const ogs_batch_config* cfg, void* 
   const char* fn = "ogs_batch_set_config";
   if (!b || !cfg) return set_error(OGS_EINVAL, "ogs_batch_set_config: NULL argument");
   if ((cfg->block != 128 && cfg->block != 256) || cfg->ctas_per_sm < 0 || cfg->solo_items < 0 ||
-      cfg->solo_streams < 1 || cfg->solo_streams > kMaxBranches)
+      cfg->solo_streams < 1 || cfg->solo_streams > kMaxBranches ||
+      (cfg->occupancy != 0 && cfg->occupancy != 2 && cfg->occupancy != 3))
     return set_error(OGS_EINVAL, "ogs_batch_set_config: block 128 or 256, ctas_per_sm >= 0, solo_items >= 0, "
-                                 "1 <= solo_streams <= 8");
+                                 "1 <= solo_streams <= 8, occupancy 2 or 3");
   ogs_status s = ensure_branches(b, cfg->solo_streams, fn);
   if (s != OGS_OK) return s;
   const int sms = b->cfg.sms;
   b->cfg = *cfg;
   b->cfg.sms = sms;
+  if (b->cfg.occupancy == 0) b->cfg.occupancy = 2;
   return apply_config(b, b->host_entries.data(), static_cast<cudaStream_t>(stream), fn);
 }
 
@@ -444,17 +447,18 @@ ogs_status ogs_batch_tune_ex(ogs_batch b, void* stream, unsigned flags, ogs_batc
     }
     return r;
   };
-  // 1) the persistent launch alone: block size x CTAs per SM
-  int maxb[2] = {4, 8};  // CTAs per SM tried for 256- and 128-thread blocks
+  // 1) the persistent launch alone: block size x register budget x CTAs per SM
   for (int bi = 0; s == OGS_OK && bi < 2; ++bi)
-    for (int c = 1; s == OGS_OK && c <= maxb[bi]; ++c) {
-      ogs_batch_config cand = saved;
-      cand.block = bi == 0 ? 256 : 128;
-      cand.ctas_per_sm = c;
-      cand.solo_items = 0;
-      cand.solo_streams = 1;
-      s = consider(cand);
-    }
+    for (int occ = 2; s == OGS_OK && occ <= 3; ++occ)
+      for (int c = 1; s == OGS_OK && c <= (bi == 0 ? 2 : 4) * occ; ++c) {
+        ogs_batch_config cand = saved;
+        cand.block = bi == 0 ? 256 : 128;
+        cand.occupancy = occ;
+        cand.ctas_per_sm = c;
+        cand.solo_items = 0;
+        cand.solo_streams = 1;
+        s = consider(cand);
+      }
   // 2) entries from a size on run alone on the single-mesh kernel, over 2, 4
   // or 8 branches: thresholds at 1/16, 1/4, 1 and 4 waves of warps of the
   // persistent grid
@@ -474,7 +478,7 @@ ogs_status ogs_batch_tune_ex(ogs_batch b, void* stream, unsigned flags, ogs_batc
   // 3) the persistent launch's CTAs per SM again, beside the chosen solo entries
   if (s == OGS_OK && best.solo_items > 0) {
     const ogs_batch_config base2 = best;
-    for (int c = 1; s == OGS_OK && c <= (base2.block == 256 ? 4 : 8); ++c) {
+    for (int c = 1; s == OGS_OK && c <= (base2.block == 256 ? 2 : 4) * base2.occupancy; ++c) {
       ogs_batch_config cand = base2;
       cand.ctas_per_sm = c;
       s = consider(cand);

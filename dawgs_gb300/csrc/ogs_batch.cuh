@@ -18,10 +18,9 @@ namespace ogsgb {
 
 constexpr int kBatchSmem = 2048;
 
-// Minimum resident CTAs per SM the batched kernel's registers must allow.
-#ifndef OGS_BATCH_MINB
-#define OGS_BATCH_MINB 2
-#endif
+// The batched kernel comes in two register budgets, chosen per launch by the
+// tuner: OCC 256-thread CTAs resident per SM (2: 107 registers, no spills;
+// 3: 80 registers, a few spilled bytes, half as many warps again).
 
 template <typename T, int D>
 __device__ __forceinline__ void fold_store_rt(int op, const WarpState& s, T* dst, int64_t stride, int K, int k,
@@ -114,8 +113,8 @@ __device__ __forceinline__ void batch_load_state(const BatchItem& it, int lane, 
 // sectors through L1/L2 (a warp walking a contiguous run of items was much
 // slower on large meshes, as for the single-mesh kernel).  The prefix
 // `starts` is staged in shared memory (dynamic, (n+1) entries) when it fits.
-template <typename T, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, OGS_BATCH_MINB * 256 / BLOCK)
+template <typename T, int BLOCK, int OCC>
+__global__ void __launch_bounds__(BLOCK, OCC * 256 / BLOCK)
     ogs_batch_kernel(const BatchEntry* __restrict__ E, const int64_t* __restrict__ starts, int n) {
   extern __shared__ int64_t s_starts[];
   const bool in_smem = n <= kBatchSmem;
@@ -162,8 +161,8 @@ __global__ void __launch_bounds__(BLOCK, OGS_BATCH_MINB * 256 / BLOCK)
   }
 }
 
-template <typename T, int BLOCK>
-inline int batch_blocks_per_sm(int n, int* sms) {
+template <typename T, int BLOCK, int OCC>
+inline int batch_blocks_per_sm(int* sms) {
   static DeviceCache bps_cache, sms_cache;
   int dev = 0;
   cudaGetDevice(&dev);
@@ -172,35 +171,53 @@ inline int batch_blocks_per_sm(int n, int* sms) {
     cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
     return s > 0 ? s : 1;
   });
-  (void)n;
   // occupancy with the largest starts table (the registers decide it)
   return bps_cache.get(dev, [] {
     int bps = 0;
-    cudaFuncSetAttribute(ogs_batch_kernel<T, BLOCK>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(ogs_batch_kernel<T, BLOCK, OCC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>((kBatchSmem + 1) * sizeof(int64_t)));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_batch_kernel<T, BLOCK>, BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_batch_kernel<T, BLOCK, OCC>, BLOCK, 0);
     return bps > 0 ? bps : 1;
   });
 }
 
-// grid <= 0: resident CTAs on every SM; grid > 0: that many CTAs.  block:
-// 128 or 256 threads per CTA.
-template <typename T>
-inline int launch_batch_typed(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid,
-                              int block, void* stream) {
-  if (nitems <= 0) return 0;
+template <typename T, int BLOCK, int OCC>
+inline int launch_batch_shape(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid,
+                              cudaStream_t st) {
   int sms = 0;
-  const int bps = block == 128 ? batch_blocks_per_sm<T, 128>(n, &sms) : batch_blocks_per_sm<T, 256>(n, &sms);
+  const int bps = batch_blocks_per_sm<T, BLOCK, OCC>(&sms);
   int64_t g = grid > 0 ? grid : static_cast<int64_t>(bps) * sms;
-  const int64_t need = (nitems + (block / 32) - 1) / (block / 32);
+  const int64_t need = (nitems + (BLOCK / 32) - 1) / (BLOCK / 32);
   if (g > need) g = need;
   const size_t smem = n <= kBatchSmem ? static_cast<size_t>(n + 1) * sizeof(int64_t) : 0;
+  ogs_batch_kernel<T, BLOCK, OCC><<<static_cast<unsigned>(g), BLOCK, smem, st>>>(E, starts, n);
+  return static_cast<int>(cudaGetLastError());
+}
+
+// Load the batched kernel of one launch shape and fill its occupancy cache
+// now, so that a server's first request does not wait for the module load.
+template <typename T, int BLOCK, int OCC>
+inline int preload_batch_shape() {
+  cudaFuncAttributes a;
+  const cudaError_t e = cudaFuncGetAttributes(&a, ogs_batch_kernel<T, BLOCK, OCC>);
+  int sms = 0;
+  if (e == cudaSuccess) batch_blocks_per_sm<T, BLOCK, OCC>(&sms);
+  return static_cast<int>(e);
+}
+
+// grid <= 0: resident CTAs on every SM; grid > 0: that many CTAs.  block:
+// 128 or 256 threads per CTA; occ: the register budget, 2 or 3 256-thread
+// CTAs per SM.
+template <typename T>
+inline int launch_batch_typed(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid,
+                              int block, int occ, void* stream) {
+  if (nitems <= 0) return 0;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (block == 128)
-    ogs_batch_kernel<T, 128><<<static_cast<unsigned>(g), 128, smem, st>>>(E, starts, n);
-  else
-    ogs_batch_kernel<T, 256><<<static_cast<unsigned>(g), 256, smem, st>>>(E, starts, n);
-  return static_cast<int>(cudaGetLastError());
+    return occ == 3 ? launch_batch_shape<T, 128, 3>(E, starts, n, nitems, grid, st)
+                    : launch_batch_shape<T, 128, 2>(E, starts, n, nitems, grid, st);
+  return occ == 3 ? launch_batch_shape<T, 256, 3>(E, starts, n, nitems, grid, st)
+                  : launch_batch_shape<T, 256, 2>(E, starts, n, nitems, grid, st);
 }
 
 }  // namespace ogsgb

@@ -297,15 +297,16 @@ int launch_i32(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern p
 int launch_i64(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern pat, void* stream);
 
 // Batched launch over `n` entries (ogs_batch.cuh); grid <= 0 = one full wave;
-// block = 128 or 256 threads per CTA.
+// block = 128 or 256 threads per CTA; occ = 2 or 3 (register budget: 256-thread
+// CTAs per SM).
 int launch_batch_f32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     void* stream);
+                     int occ, void* stream);
 int launch_batch_f64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     void* stream);
+                     int occ, void* stream);
 int launch_batch_i32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     void* stream);
+                     int occ, void* stream);
 int launch_batch_i64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     void* stream);
+                     int occ, void* stream);
 
 // Device and page-locked host allocations (ogs_alloc.cpp): counted, and made
 // to fail on demand by ogs_debug_fail_alloc.  Every allocation of the library
@@ -322,6 +323,13 @@ template <typename T>
 inline cudaError_t host_malloc(T** p, size_t bytes) {
   return host_malloc_raw(reinterpret_cast<void**>(p), bytes);
 }
+
+// Load the batched kernel the server launches (256 threads, 2 CTAs per SM)
+// ahead of its first use.
+int preload_batch_f32();
+int preload_batch_f64();
+int preload_batch_i32();
+int preload_batch_i64();
 
 // Thread-local error message (ogs_capi.cpp).
 ogs_status set_error(ogs_status s, const std::string& msg);

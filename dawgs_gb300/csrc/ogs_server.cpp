@@ -61,8 +61,10 @@ constexpr int kAdmitWindow = 64;
 constexpr int kMaxPassOvers = 16;
 // Fields up to this size go to the small lane.
 constexpr size_t kSmallBytes = size_t(4) << 20;
-// Launch tables per server (shared by both lanes).
+// Launch tables per server (shared by both lanes), and completion events made
+// at creation (more are made when requests in flight need them).
 constexpr int kTableSlots = 64;
+constexpr int kSpareEvents = 512;
 
 enum ReqState : int { kPending = 0, kInFlight = 1, kDone = 2, kCancelled = 3 };
 
@@ -170,10 +172,10 @@ namespace {
 
 int batch_launch(int type, const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, cudaStream_t st) {
   switch (type) {
-    case OGS_FLOAT: return launch_batch_f32(E, starts, n, nitems, 0, 256, st);
-    case OGS_DOUBLE: return launch_batch_f64(E, starts, n, nitems, 0, 256, st);
-    case OGS_INT32: return launch_batch_i32(E, starts, n, nitems, 0, 256, st);
-    default: return launch_batch_i64(E, starts, n, nitems, 0, 256, st);
+    case OGS_FLOAT: return launch_batch_f32(E, starts, n, nitems, 0, 256, 2, st);
+    case OGS_DOUBLE: return launch_batch_f64(E, starts, n, nitems, 0, 256, 2, st);
+    case OGS_INT32: return launch_batch_i32(E, starts, n, nitems, 0, 256, 2, st);
+    default: return launch_batch_i64(E, starts, n, nitems, 0, 256, 2, st);
   }
 }
 
@@ -461,6 +463,24 @@ ogs_status ogs_server_create(ogs_server* out, const ogs_server_config* cfg) {
     t.h_starts = reinterpret_cast<int64_t*>(s->h_tables + j * (eb + sb) + eb);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&t.done, cudaEventDisableTiming);
   }
+  // Everything a first request would otherwise set up on the worker's path:
+  // the batched kernels' modules (loaded lazily by the runtime on first use,
+  // milliseconds each, during which every request waits), the completion
+  // events, and each stream's first operation.
+  if (e == cudaSuccess) e = static_cast<cudaError_t>(preload_batch_f32());
+  if (e == cudaSuccess) e = static_cast<cudaError_t>(preload_batch_f64());
+  if (e == cudaSuccess) e = static_cast<cudaError_t>(preload_batch_i32());
+  if (e == cudaSuccess) e = static_cast<cudaError_t>(preload_batch_i64());
+  for (int j = 0; e == cudaSuccess && j < kSpareEvents; ++j) {
+    cudaEvent_t ev = nullptr;
+    e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) s->spare_events.push_back(ev);
+  }
+  for (Lane& l : s->lanes)
+    for (cudaStream_t st : {l.in, l.compute, l.out}) {
+      if (e == cudaSuccess) e = cudaEventRecord(l.copied, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    }
   if (e != cudaSuccess) {
     cudaGetLastError();
     destroy(s);
