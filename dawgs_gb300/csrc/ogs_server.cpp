@@ -61,6 +61,14 @@ constexpr int kAdmitWindow = 64;
 constexpr int kMaxPassOvers = 16;
 // Fields up to this size go to the small lane.
 constexpr size_t kSmallBytes = size_t(4) << 20;
+// Launches a lane keeps on the GPU at once.  While they run, newly admitted
+// requests wait in the lane and go together in its next launch: under load
+// the batches grow and the per-launch costs are shared; with nothing running
+// a request is launched at once.
+#ifndef OGS_SERVER_LANE_LAUNCHES
+#define OGS_SERVER_LANE_LAUNCHES 2
+#endif
+static_assert(OGS_SERVER_LANE_LAUNCHES >= 1 && OGS_SERVER_LANE_LAUNCHES < 8, "a lane rotates 8 turn events");
 // Launch tables per server (shared by both lanes), and completion events made
 // at creation (more are made when requests in flight need them).
 constexpr int kTableSlots = 64;
@@ -136,6 +144,9 @@ struct Lane {
   cudaEvent_t copied = nullptr;  // all of a turn's copies in are done
   std::vector<Req*> ready;       // admitted, not yet launched (worker only)
   std::deque<Req*> outstanding;  // launched, in copy-out order (worker only)
+  std::deque<cudaEvent_t> running;  // its turns' launches not yet finished, in order (worker only)
+  cudaEvent_t turn_done[8] = {};     // recorded after each turn's launches, used in rotation
+  int next_turn_event = 0;
 };
 
 }  // namespace
@@ -280,6 +291,12 @@ int launch_group(ogs_server_s* s, Lane& lane, TableSlot& slot, const std::vector
 // Launch what a lane has ready, when enough table slots are free.
 int launch_lane(ogs_server_s* s, Lane& lane) {
   if (lane.ready.empty()) return 0;
+  while (!lane.running.empty()) {
+    const cudaError_t q = cudaEventQuery(lane.running.front());
+    if (q == cudaErrorNotReady) break;
+    lane.running.pop_front();
+  }
+  if (static_cast<int>(lane.running.size()) >= OGS_SERVER_LANE_LAUNCHES) return 0;  // next turn, a larger batch
   std::vector<Req*> grp[4];
   int groups = 0;
   for (Req* q : lane.ready) {
@@ -295,6 +312,12 @@ int launch_lane(ogs_server_s* s, Lane& lane) {
   int j = 0;
   for (int type = OGS_FLOAT; !e && type <= OGS_INT64; ++type)
     if (!grp[type].empty()) e = launch_group(s, lane, *slots[j++], grp[type], type);
+  if (!e) {
+    cudaEvent_t ev = lane.turn_done[lane.next_turn_event];
+    lane.next_turn_event = (lane.next_turn_event + 1) % 8;
+    e = cudaEventRecord(ev, lane.compute);
+    if (!e) lane.running.push_back(ev);
+  }
   lane.ready.clear();
   return e;
 }
@@ -416,6 +439,8 @@ void destroy(ogs_server_s* s) {
     for (cudaStream_t st : {l.in, l.compute, l.out})
       if (st) cudaStreamDestroy(st);
     if (l.copied) cudaEventDestroy(l.copied);
+    for (cudaEvent_t ev : l.turn_done)
+      if (ev) cudaEventDestroy(ev);
   }
   dev_free(s->pool_base);
   delete s;
@@ -448,6 +473,8 @@ ogs_status ogs_server_create(ogs_server* out, const ogs_server_config* cfg) {
     for (cudaStream_t* st : {&l.in, &l.compute, &l.out})
       if (e == cudaSuccess) e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&l.copied, cudaEventDisableTiming);
+    for (cudaEvent_t& ev : l.turn_done)
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
   }
   // the launch tables of all slots: entries then starts, 256-byte aligned
   const size_t eb = (sizeof(BatchEntry) * cfg->max_batch + 255) / 256 * 256;
