@@ -88,6 +88,7 @@ SIGNATURES = {
     "ogs_server_drain": (_i, [_vp]),
     "ogs_server_latencies": (_i, [_vp, _i64, _i64, _vp, _vp]),
     "ogs_server_counters": (_i, [_vp, _vp, _vp]),
+    "ogs_server_get_stats": (_i, [_vp, _vp]),
     "ogs_server_free": (_i, [_vp]),
     "ogs_last_error_string": (C.c_char_p, []),
     "ogs_version": (_i, []),
@@ -138,6 +139,11 @@ class OgsExchange(C.Structure):
 
 class OgsServerConfig(C.Structure):
     _fields_ = [("field_budget_bytes", C.c_int64), ("max_inflight", C.c_int32), ("max_batch", C.c_int32)]
+
+
+class OgsServerStats(C.Structure):
+    _fields_ = [("passes", C.c_int64), ("gaps_over_1ms", C.c_int64), ("launches_over_1ms", C.c_int64),
+                ("max_gap_ms", C.c_double), ("max_launch_ms", C.c_double), ("max_retire_ms", C.c_double)]
 
 
 class OgsServerRequest(C.Structure):

@@ -35,10 +35,6 @@
 
 namespace ogsgb {
 
-#ifndef OGS_KMULTI_CTAS
-#define OGS_KMULTI_CTAS 0
-#endif
-
 #ifndef OGS_ASYNC_STAGES
 #define OGS_ASYNC_STAGES 2
 #endif
@@ -265,8 +261,6 @@ inline int async_grid(int64_t nitems) {
                            static_cast<int>(async_smem_bytes<T>()));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_async_kernel<T, OP, MODE, KL, PLAIN>, kBlock,
                                                   async_smem_bytes<T>());
-    // k > 1: a cap on the CTAs per SM (OGS_KMULTI_CTAS; 0 = as many as fit)
-    if (KL != kK1 && OGS_KMULTI_CTAS > 0 && bps > OGS_KMULTI_CTAS) bps = OGS_KMULTI_CTAS;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     return (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1);
   });

@@ -176,6 +176,7 @@ struct ogs_server_s {
   std::thread worker;
   std::atomic<bool> stop{false};
   std::string error;
+  ogs_server_stats stats{};  // the worker's own timing (s->mu held to read or write)
 };
 
 namespace ogsgb {
@@ -384,8 +385,22 @@ double admit(ogs_server_s* s, double now) {
 
 void worker_loop(ogs_server_s* s) {
   cudaSetDevice(s->device);
+  double t_prev = now_s();
   while (true) {
+    // the worker's timing: gaps between passes (sleeping or descheduled) and
+    // the time spent in CUDA calls
+    const double t_pass = now_s();
     for (Lane& l : s->lanes) retire(s, l);
+    const double t_retired = now_s();
+    {
+      std::lock_guard<std::mutex> g(s->mu);
+      ogs_server_stats& w = s->stats;
+      w.passes++;
+      w.max_gap_ms = std::max(w.max_gap_ms, (t_pass - t_prev) * 1e3);
+      w.max_retire_ms = std::max(w.max_retire_ms, (t_retired - t_pass) * 1e3);
+      if (t_pass - t_prev > 1e-3) w.gaps_over_1ms++;
+    }
+    t_prev = t_pass;
     bool idle;
     {
       std::unique_lock<std::mutex> lk(s->mu);
@@ -412,11 +427,13 @@ void worker_loop(ogs_server_s* s) {
       }
     }
     for (Lane& l : s->lanes) {
+      const double t0 = now_s();
       const int e = launch_lane(s, l);
-      if (e) {
-        std::lock_guard<std::mutex> g(s->mu);
-        if (s->error.empty()) s->error = cudaGetErrorString(static_cast<cudaError_t>(e));
-      }
+      const double dt = now_s() - t0;
+      std::lock_guard<std::mutex> g(s->mu);
+      s->stats.max_launch_ms = std::max(s->stats.max_launch_ms, dt * 1e3);
+      if (dt > 1e-3) s->stats.launches_over_1ms++;
+      if (e && s->error.empty()) s->error = cudaGetErrorString(static_cast<cudaError_t>(e));
     }
     {
       // a lane left waiting for a table slot: let launches finish
@@ -671,6 +688,13 @@ ogs_status ogs_server_times(ogs_server s, int64_t first, int64_t n, double* arri
 
 ogs_status ogs_server_latencies(ogs_server s, int64_t first, int64_t n, double* arrival, double* done) {
   return ogs_server_times(s, first, n, arrival, nullptr, done);
+}
+
+ogs_status ogs_server_get_stats(ogs_server s, ogs_server_stats* out) {
+  if (!s || !out) return set_error(OGS_EINVAL, "ogs_server_get_stats: NULL argument");
+  std::lock_guard<std::mutex> g(s->mu);
+  *out = s->stats;
+  return OGS_OK;
 }
 
 ogs_status ogs_server_counters(ogs_server s, int64_t* launches, int64_t* batched_requests) {

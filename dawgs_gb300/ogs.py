@@ -548,6 +548,12 @@ class ogs_server_t:
         check(lib().ogs_server_times(self._s, int(first), int(n), a.ctypes.data, lt.ctypes.data, d.ctypes.data))
         return (a, lt, d) if launched else (a, d)
 
+    def stats(self) -> dict:
+        """The worker thread's timing (passes, long gaps, long launches)."""
+        st = _lib.OgsServerStats()
+        check(lib().ogs_server_get_stats(self._s, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in st._fields_}
+
     def counters(self):
         l, b = C.c_int64(), C.c_int64()
         check(lib().ogs_server_counters(self._s, C.byref(l), C.byref(b)))

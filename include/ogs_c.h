@@ -418,6 +418,18 @@ ogs_status ogs_server_latencies(ogs_server s, int64_t first, int64_t n, double *
 ogs_status ogs_server_times(ogs_server s, int64_t first, int64_t n, double *arrival, double *launched,
                             double *done);
 ogs_status ogs_server_counters(ogs_server s, int64_t *launches, int64_t *batched_requests);
+/* The worker thread's own timing, for finding where a latency tail comes
+ * from: long gaps between its passes mean it slept or was descheduled, long
+ * launches or retire passes mean CUDA calls blocked. */
+typedef struct {
+  int64_t passes;            /* passes of the worker loop */
+  int64_t gaps_over_1ms;     /* passes that began more than 1 ms after the previous one */
+  int64_t launches_over_1ms; /* lane launches (copies, tables, kernels) that took over 1 ms of host time */
+  double max_gap_ms;
+  double max_launch_ms;
+  double max_retire_ms;      /* longest pass over the completion events */
+} ogs_server_stats;
+ogs_status ogs_server_get_stats(ogs_server s, ogs_server_stats *out);
 /* Finishes outstanding requests, then releases the server. */
 ogs_status ogs_server_free(ogs_server s);
 
