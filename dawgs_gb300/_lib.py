@@ -121,7 +121,7 @@ TUNE_NO_CACHE = 1
 class OgsBatchConfig(C.Structure):
     _fields_ = [("block", C.c_int32), ("ctas_per_sm", C.c_int32), ("solo_items", C.c_int64),
                 ("solo_streams", C.c_int32), ("sms", C.c_int32), ("from_cache", C.c_int32),
-                ("occupancy", C.c_int32), ("ms", C.c_double)]
+                ("occupancy", C.c_int32), ("ms", C.c_double), ("pipeline", C.c_int32), ("reserved", C.c_int32)]
 
 
 class OgsHaloCounts(C.Structure):

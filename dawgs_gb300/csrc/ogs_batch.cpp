@@ -158,10 +158,14 @@ int launch_all(ogs_batch_s* b, const BatchEntry* fields, cudaStream_t st) {
     const int64_t nitems = b->starts.back();
     const int grid = b->cfg.ctas_per_sm > 0 ? b->cfg.ctas_per_sm * std::max(1, b->cfg.sms) : 0;
     switch (b->type) {
-      case OGS_FLOAT: e = launch_batch_f32(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy, st); break;
-      case OGS_DOUBLE: e = launch_batch_f64(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy, st); break;
-      case OGS_INT32: e = launch_batch_i32(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy, st); break;
-      default: e = launch_batch_i64(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy, st); break;
+      case OGS_FLOAT: e = launch_batch_f32(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy,
+                                             b->cfg.pipeline, st); break;
+      case OGS_DOUBLE: e = launch_batch_f64(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy,
+                                             b->cfg.pipeline, st); break;
+      case OGS_INT32: e = launch_batch_i32(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy,
+                                             b->cfg.pipeline, st); break;
+      default: e = launch_batch_i64(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy,
+                                             b->cfg.pipeline, st); break;
     }
     for (size_t q = 0; !e && q < b->general.size(); ++q) {
       const int i = b->general[q];
@@ -248,6 +252,7 @@ ogs_status ogs_batch_create(ogs_batch* out, int type, const ogs_batch_entry* ent
     else if (!e.h->distinct_cols) bad = "a local node appears in two rows of this operator's map";
     else if (e.h->device != dev) bad = "handle lives on another device";
     else if (e.k < 1) bad = "k must be >= 1";
+    else if (static_cast<int64_t>(e.h->dmaps.nwtiles) * e.k > INT32_MAX) bad = "more than 2^31 work items";
     else if (e.op < OGS_ADD || e.op > OGS_MIN) bad = "unknown op";
     else if (e.trans < OGS_SYM || e.trans > OGS_TRANS) bad = "unknown transpose";
     else if (!e.d_v && e.h->N > 0) bad = "field is NULL";
@@ -353,9 +358,10 @@ ogs_status ogs_batch_set_config(ogs_batch b, const ogs_batch_config* cfg, void* 
   if (!b || !cfg) return set_error(OGS_EINVAL, "ogs_batch_set_config: NULL argument");
   if ((cfg->block != 128 && cfg->block != 256) || cfg->ctas_per_sm < 0 || cfg->solo_items < 0 ||
       cfg->solo_streams < 1 || cfg->solo_streams > kMaxBranches ||
-      (cfg->occupancy != 0 && cfg->occupancy != 2 && cfg->occupancy != 3))
+      (cfg->occupancy != 0 && cfg->occupancy != 2 && cfg->occupancy != 3) || cfg->pipeline < 0 ||
+      cfg->pipeline > 1 || (cfg->pipeline == 1 && cfg->block != 256))
     return set_error(OGS_EINVAL, "ogs_batch_set_config: block 128 or 256, ctas_per_sm >= 0, solo_items >= 0, "
-                                 "1 <= solo_streams <= 8, occupancy 2 or 3");
+                                 "1 <= solo_streams <= 8, occupancy 2 or 3, pipeline 0 or 1 (1: block 256)");
   ogs_status s = ensure_branches(b, cfg->solo_streams, fn);
   if (s != OGS_OK) return s;
   const int sms = b->cfg.sms;
@@ -447,18 +453,21 @@ ogs_status ogs_batch_tune_ex(ogs_batch b, void* stream, unsigned flags, ogs_batc
     }
     return r;
   };
-  // 1) the persistent launch alone: block size x register budget x CTAs per SM
-  for (int bi = 0; s == OGS_OK && bi < 2; ++bi)
-    for (int occ = 2; s == OGS_OK && occ <= 3; ++occ)
-      for (int c = 1; s == OGS_OK && c <= (bi == 0 ? 2 : 4) * occ; ++c) {
-        ogs_batch_config cand = saved;
-        cand.block = bi == 0 ? 256 : 128;
-        cand.occupancy = occ;
-        cand.ctas_per_sm = c;
-        cand.solo_items = 0;
-        cand.solo_streams = 1;
-        s = consider(cand);
-      }
+  // 1) the persistent launch alone: pipeline x block size x register budget x
+  // CTAs per SM (the ring pipeline has 256-thread blocks only)
+  for (int pipe = 0; s == OGS_OK && pipe <= 1; ++pipe)
+    for (int bi = 0; s == OGS_OK && bi < (pipe ? 1 : 2); ++bi)
+      for (int occ = 2; s == OGS_OK && occ <= 3; ++occ)
+        for (int c = 1; s == OGS_OK && c <= (bi == 0 ? 2 : 4) * occ; ++c) {
+          ogs_batch_config cand = saved;
+          cand.pipeline = pipe;
+          cand.block = bi == 0 ? 256 : 128;
+          cand.occupancy = occ;
+          cand.ctas_per_sm = c;
+          cand.solo_items = 0;
+          cand.solo_streams = 1;
+          s = consider(cand);
+        }
   // 2) entries from a size on run alone on the single-mesh kernel, over 2, 4
   // or 8 branches: thresholds at 1/16, 1/4, 1 and 4 waves of warps of the
   // persistent grid

@@ -12,6 +12,7 @@
 // (warp-uniform), so one launch serves entries with different ops.
 #pragma once
 
+#include "ogs_async.cuh"
 #include "ogs_warp.cuh"
 
 namespace ogsgb {
@@ -194,6 +195,185 @@ inline int launch_batch_shape(const BatchEntry* E, const int64_t* starts, int n,
   return static_cast<int>(cudaGetLastError());
 }
 
+// ---- the same batch on the cp.async ring (ogs_async.cuh) ----
+// Each warp keeps two items' value gathers and a third item's column ids in
+// flight, as the single-mesh kernel does.  To leave room for that in 80
+// registers, a lookahead item is carried as its position only -- entry,
+// record, component, degree -- and its field, op and record are read again
+// from the entry table and the record (L1-resident) where they are needed.
+struct BatchPos {
+  int32_t e, r, k, d;
+};
+
+__device__ __forceinline__ BatchPos batch_pos(const BatchEntry* E, const int64_t* st, int n, int64_t i) {
+  BatchPos p;
+  p.e = batch_entry_of(st, n, i);
+  const int K = E[p.e].K;
+  const int32_t local = static_cast<int32_t>(i - st[p.e]);  // items of one entry fit 32 bits
+  p.r = local / K;
+  p.k = local - p.r * K;
+  p.d = E[p.e].recs[p.r].bucket_count >> 16;
+  return p;
+}
+
+template <int D>
+__device__ __forceinline__ void batch_state_at(const BatchEntry* E, const BatchPos& p, int lane, WarpState& s) {
+  const BatchEntry& be = E[p.e];
+  const WarpRec& w = be.recs[p.r];
+  DevBucket b;
+  b.cols = w.cols;
+  b.rows = nullptr;
+  b.nmask = nullptr;
+  b.n = INT32_MAX;
+  b.nP = w.nP;
+  b.stride = w.stride;
+  b.nnodes = INT32_MAX;
+  b.nrows = INT32_MAX;
+  b.err = nullptr;
+  Tile t;
+  t.bucket = D;
+  t.begin = w.begin;
+  t.count = w.bucket_count & 0xFFFF;
+  t.first_row = 0;
+  const Pattern pat{be.gather_n, be.scatter_n, be.limit_n};
+  warp_load_state<kModeGS, D>(b, t, be.wemask, p.r, be.use_mask != 0, pat, lane, s);
+}
+
+template <typename T>
+OGS_HD constexpr size_t batch_ring_bytes() {  // 8 warps x 2 stages x kWarpSlots x 32 values
+  return static_cast<size_t>(kBlock / 32) * kAsyncStages * kWarpSlots * 32 * sizeof(T);
+}
+
+template <typename T, int OCC>
+__global__ void __launch_bounds__(kBlock, OCC)
+    ogs_batch_async_kernel(const BatchEntry* __restrict__ E, const int64_t* __restrict__ starts, int n) {
+  extern __shared__ __align__(16) unsigned char batch_smem[];
+  const int lane = static_cast<int>(threadIdx.x) & 31;
+  const int warp = static_cast<int>(threadIdx.x) >> 5;
+  T* ring = reinterpret_cast<T*>(batch_smem) + static_cast<size_t>(warp) * kAsyncStages * kWarpSlots * 32;
+  int64_t* s_starts = reinterpret_cast<int64_t*>(batch_smem + batch_ring_bytes<T>());
+  const bool in_smem = n <= kBatchSmem;
+  if (in_smem)
+    for (int j = threadIdx.x; j <= n; j += kBlock) s_starts[j] = starts[j];
+  __syncthreads();
+  const int64_t* st = in_smem ? s_starts : starts;
+  const int64_t nitems = st[n];
+  const int64_t W = static_cast<int64_t>(gridDim.x) * (kBlock / 32);
+  int64_t i = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + warp;
+  if (i >= nitems) return;
+
+  BatchPos cur = batch_pos(E, st, n, i), nxt{}, nn{};
+  const bool has1 = i + W < nitems;
+  if (has1) nxt = batch_pos(E, st, n, i + W);
+  if (i + 2 * W < nitems) nn = batch_pos(E, st, n, i + 2 * W);
+  WarpState scur, snxt;
+#define OGS_BA_STATE(D, P, S) batch_state_at<D>(E, P, lane, S)
+#define OGS_BA_CUR(D) OGS_BA_STATE(D, cur, scur)
+  OGS_DEGREE_SWITCH(cur.d, OGS_BA_CUR)
+#undef OGS_BA_CUR
+  if (has1) {
+#define OGS_BA_NXT(D) OGS_BA_STATE(D, nxt, snxt)
+    OGS_DEGREE_SWITCH(nxt.d, OGS_BA_NXT)
+#undef OGS_BA_NXT
+  }
+  {
+    const BatchEntry& be = E[cur.e];
+    const T* src = static_cast<const T*>(be.v) + cur.k;
+    const bool gmask = be.gather_n != 0;
+#define OGS_BA_ISSUE0(D) async_issue_vals<T, kModeGS, D>(scur, src, nullptr, be.K, be.K, cur.k, gmask, lane, ring)
+    OGS_DEGREE_SWITCH(cur.d, OGS_BA_ISSUE0)
+#undef OGS_BA_ISSUE0
+  }
+  cp_async_commit();
+
+  int stage = 0;
+  for (;;) {
+    const bool more1 = i + W < nitems;
+    const bool more2 = i + 2 * W < nitems;
+    const int nstage = stage == kAsyncStages - 1 ? 0 : stage + 1;
+    if (more1) {
+      const BatchEntry& be = E[nxt.e];
+      const T* src1 = static_cast<const T*>(be.v) + nxt.k;
+      const bool gmask1 = be.gather_n != 0;
+      T* st1 = ring + nstage * (kWarpSlots * 32);
+#define OGS_BA_ISSUE1(D) async_issue_vals<T, kModeGS, D>(snxt, src1, nullptr, be.K, be.K, nxt.k, gmask1, lane, st1)
+      OGS_DEGREE_SWITCH(nxt.d, OGS_BA_ISSUE1)
+#undef OGS_BA_ISSUE1
+    }
+    cp_async_commit();
+    WarpState snn;
+    BatchPos n3{};
+    if (more2) {
+#define OGS_BA_NN(D) OGS_BA_STATE(D, nn, snn)
+      OGS_DEGREE_SWITCH(nn.d, OGS_BA_NN)
+#undef OGS_BA_NN
+      if (i + 3 * W < nitems) n3 = batch_pos(E, st, n, i + 3 * W);
+    }
+    cp_async_wait<1>();  // the gathers of item i are in
+    {
+      const BatchEntry& be = E[cur.e];
+      const int K = be.K;
+      T* dst = static_cast<T*>(be.v) + cur.k;
+      const bool gmask = be.gather_n != 0;
+      const int smode = be.scatter_n;
+      const int op = be.op;
+      const T* st0 = ring + stage * (kWarpSlots * 32);
+      T V[kWarpSlots];
+#define OGS_BA_FOLD(D)                                                            \
+  do {                                                                            \
+    async_read_vals<T, kModeGS, D>(scur, gmask, lane, st0, V);                    \
+    fold_store_rt<T, D>(op, scur, dst, K, K, cur.k, gmask, smode, lane, V);       \
+  } while (0)
+      OGS_DEGREE_SWITCH(cur.d, OGS_BA_FOLD)
+#undef OGS_BA_FOLD
+    }
+    if (!more1) break;
+    i += W;
+    stage = nstage;
+    cur = nxt;
+    scur = snxt;
+    nxt = nn;
+    snxt = snn;
+    nn = n3;
+  }
+  cp_async_wait<0>();
+#undef OGS_BA_STATE
+}
+
+template <typename T, int OCC>
+inline int batch_async_blocks_per_sm(int* sms) {
+  static DeviceCache bps_cache, sms_cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  *sms = sms_cache.get(dev, [dev] {
+    int s = 0;
+    cudaDeviceGetAttribute(&s, cudaDevAttrMultiProcessorCount, dev);
+    return s > 0 ? s : 1;
+  });
+  return bps_cache.get(dev, [] {
+    int bps = 0;
+    const size_t smem = batch_ring_bytes<T>() + (kBatchSmem + 1) * sizeof(int64_t);
+    cudaFuncSetAttribute(ogs_batch_async_kernel<T, OCC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(smem));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_batch_async_kernel<T, OCC>, kBlock,
+                                                  batch_ring_bytes<T>() + 257 * sizeof(int64_t));
+    return bps > 0 ? bps : 1;
+  });
+}
+
+template <typename T, int OCC>
+inline int launch_batch_async_shape(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid,
+                                    cudaStream_t st) {
+  int sms = 0;
+  const int bps = batch_async_blocks_per_sm<T, OCC>(&sms);
+  int64_t g = grid > 0 ? grid : static_cast<int64_t>(bps) * sms;
+  const int64_t need = (nitems + (kBlock / 32) - 1) / (kBlock / 32);
+  if (g > need) g = need;
+  const size_t smem = batch_ring_bytes<T>() + (n <= kBatchSmem ? static_cast<size_t>(n + 1) * sizeof(int64_t) : 0);
+  ogs_batch_async_kernel<T, OCC><<<static_cast<unsigned>(g), kBlock, smem, st>>>(E, starts, n);
+  return static_cast<int>(cudaGetLastError());
+}
+
 // Load the batched kernel of one launch shape and fill its occupancy cache
 // now, so that a server's first request does not wait for the module load.
 template <typename T, int BLOCK, int OCC>
@@ -207,12 +387,16 @@ inline int preload_batch_shape() {
 
 // grid <= 0: resident CTAs on every SM; grid > 0: that many CTAs.  block:
 // 128 or 256 threads per CTA; occ: the register budget, 2 or 3 256-thread
-// CTAs per SM.
+// CTAs per SM; pipe 0: the register pipeline, 1: the cp.async ring.
+// pipe 1: the cp.async ring (256-thread blocks; occ 2 or 3).
 template <typename T>
 inline int launch_batch_typed(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid,
-                              int block, int occ, void* stream) {
+                              int block, int occ, int pipe, void* stream) {
   if (nitems <= 0) return 0;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (pipe == 1)
+    return occ == 3 ? launch_batch_async_shape<T, 3>(E, starts, n, nitems, grid, st)
+                    : launch_batch_async_shape<T, 2>(E, starts, n, nitems, grid, st);
   if (block == 128)
     return occ == 3 ? launch_batch_shape<T, 128, 3>(E, starts, n, nitems, grid, st)
                     : launch_batch_shape<T, 128, 2>(E, starts, n, nitems, grid, st);

@@ -298,15 +298,15 @@ int launch_i64(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern p
 
 // Batched launch over `n` entries (ogs_batch.cuh); grid <= 0 = one full wave;
 // block = 128 or 256 threads per CTA; occ = 2 or 3 (register budget: 256-thread
-// CTAs per SM).
+// CTAs per SM); pipe = 0 register pipeline, 1 cp.async ring (256 threads).
 int launch_batch_f32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     int occ, void* stream);
+                     int occ, int pipe, void* stream);
 int launch_batch_f64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     int occ, void* stream);
+                     int occ, int pipe, void* stream);
 int launch_batch_i32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     int occ, void* stream);
+                     int occ, int pipe, void* stream);
 int launch_batch_i64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     int occ, void* stream);
+                     int occ, int pipe, void* stream);
 
 // Device and page-locked host allocations (ogs_alloc.cpp): counted, and made
 // to fail on demand by ogs_debug_fail_alloc.  Every allocation of the library

@@ -184,10 +184,10 @@ namespace {
 
 int batch_launch(int type, const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, cudaStream_t st) {
   switch (type) {
-    case OGS_FLOAT: return launch_batch_f32(E, starts, n, nitems, 0, 256, 2, st);
-    case OGS_DOUBLE: return launch_batch_f64(E, starts, n, nitems, 0, 256, 2, st);
-    case OGS_INT32: return launch_batch_i32(E, starts, n, nitems, 0, 256, 2, st);
-    default: return launch_batch_i64(E, starts, n, nitems, 0, 256, 2, st);
+    case OGS_FLOAT: return launch_batch_f32(E, starts, n, nitems, 0, 256, 2, 0, st);
+    case OGS_DOUBLE: return launch_batch_f64(E, starts, n, nitems, 0, 256, 2, 0, st);
+    case OGS_INT32: return launch_batch_i32(E, starts, n, nitems, 0, 256, 2, 0, st);
+    default: return launch_batch_i64(E, starts, n, nitems, 0, 256, 2, 0, st);
   }
 }
 

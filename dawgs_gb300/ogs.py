@@ -440,7 +440,7 @@ class ogs_batch_t:
 
     @staticmethod
     def _cfg_dict(c):
-        return {"block": c.block, "occupancy": c.occupancy or 2, "ctas_per_sm": c.ctas_per_sm,
+        return {"pipeline": c.pipeline, "block": c.block, "occupancy": c.occupancy or 2, "ctas_per_sm": c.ctas_per_sm,
                 "solo_items": c.solo_items, "solo_streams": c.solo_streams, "sms": c.sms,
                 "from_cache": bool(c.from_cache), "ms": c.ms}
 
@@ -450,9 +450,10 @@ class ogs_batch_t:
         check(lib().ogs_batch_get_config(self._b, C.byref(c)))
         return self._cfg_dict(c)
 
-    def set_config(self, block=256, ctas_per_sm=0, solo_items=0, solo_streams=1, occupancy=2, stream=None):
+    def set_config(self, block=256, ctas_per_sm=0, solo_items=0, solo_streams=1, occupancy=2, pipeline=0,
+                   stream=None):
         c = _lib.OgsBatchConfig(int(block), int(ctas_per_sm), int(solo_items), int(solo_streams), 0, 0,
-                                int(occupancy), 0.0)
+                                int(occupancy), 0.0, int(pipeline), 0)
         check(lib().ogs_batch_set_config(self._b, C.byref(c), _stream_of(stream)))
 
     @property

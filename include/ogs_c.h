@@ -326,6 +326,10 @@ typedef struct {
   int32_t occupancy;    /* register budget of the persistent launch: 2 or 3 256-thread
                            CTAs per SM (0 = 2) */
   double ms;            /* (out) the tuner's time for one batch call, ms */
+  int32_t pipeline;     /* persistent launch: 0 values in registers (one item in flight
+                           per warp), 1 values staged by cp.async in shared memory (two
+                           items in flight; 256-thread blocks) */
+  int32_t reserved;
 } ogs_batch_config;
 #define OGS_BATCH_GRAPH 1u  /* capture the launch in a CUDA graph on first use, replay after */
 ogs_status ogs_batch_create(ogs_batch *out, int type, const ogs_batch_entry *entries, int n, unsigned flags);
@@ -336,8 +340,8 @@ ogs_status ogs_batch_gather_scatter(ogs_batch b, void *stream);
 ogs_status ogs_batch_get_config(ogs_batch b, ogs_batch_config *cfg);
 /* Use this configuration (its outputs are ignored); synchronises `stream`. */
 ogs_status ogs_batch_set_config(ogs_batch b, const ogs_batch_config *cfg, void *stream);
-/* The tuner: times candidate configurations (block size x register budget x
- * CTAs per SM of the persistent launch, then size thresholds x branches for the single-mesh
+/* The tuner: times candidate configurations (pipeline x block size x register
+ * budget x CTAs per SM of the persistent launch, then size thresholds x branches for the single-mesh
  * launches, then CTAs per SM again) on scratch copies of the fields -- the
  * caller's fields are read once and never written -- and keeps the fastest.
  * The choice is cached for the process under a key of the value type, the SM

@@ -90,9 +90,11 @@ def test_batch_of_one_equals_plain_call(cuda, oracle_mod):
     assert torch.equal(a, c)
 
 
-@pytest.mark.parametrize("cfg", [dict(), dict(block=128, ctas_per_sm=3), dict(solo_items=1, solo_streams=3),
-                                 dict(solo_items=40, solo_streams=2, ctas_per_sm=1)],
-                         ids=["default", "block128", "all-solo", "mixed"])
+@pytest.mark.parametrize("cfg", [dict(), dict(block=128, ctas_per_sm=3), dict(occupancy=3, ctas_per_sm=6),
+                                 dict(block=128, occupancy=3, ctas_per_sm=5),
+                                 dict(pipeline=1), dict(pipeline=1, occupancy=3, ctas_per_sm=2),
+                                 dict(solo_items=1, solo_streams=3), dict(solo_items=40, solo_streams=8, ctas_per_sm=1)],
+                         ids=["default", "block128", "occ3", "block128-occ3", "ring", "ring-occ3", "all-solo", "mixed"])
 def test_batch_configurations_give_the_same_results(cuda, oracle_mod, cfg):
     """Every configuration the tuner may choose -- block size, CTAs per SM,
     entries run alone on the single-mesh kernel over parallel graph branches
