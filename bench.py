@@ -454,11 +454,23 @@ def run_served(a, dev, L, stream):
         srv.drain()
         ta, tl, td = srv.times(0, n, launched=True)
         launches, _ = srv.counters()
+        worker = srv.stats()
         srv.Free()
         lat = (td - ta) * 1e3
         span = td.max() - ta.min()
         out = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+               "p999_ms": float(np.percentile(lat, 99.9)),
                "dofs_per_s": dofs / span, "requests_per_s": n / span, "launches": int(launches)}
+        # when the slow requests arrived (50 ms bins from the first arrival)
+        # and whether the worker itself stalled: a tail made of a few bins, at
+        # a regular period, with long gaps between the worker's passes or
+        # long CUDA calls, comes from outside the service (the host or the
+        # driver), not from queueing in it
+        slow = lat > 5.0
+        bins = np.unique(np.floor((ta[slow] - ta.min()) / 0.05).astype(np.int64))
+        out["over_5ms"] = {"share": float(slow.mean()), "bins_50ms": int(bins.size),
+                           "first_bins": [int(b) for b in bins[:12]]}
+        out["worker"] = {k: (round(v, 3) if isinstance(v, float) else v) for k, v in worker.items()}
         # where the time goes: waiting to be launched (admission, worker) and
         # from launch to completion (copies and kernels), small and large
         # fields apart (the server's two lanes split at 4 MiB)
