@@ -39,6 +39,12 @@ namespace ogsgb {
 #define OGS_ASYNC_STAGES 2
 #endif
 constexpr int kAsyncStages = OGS_ASYNC_STAGES;
+// k > 1 interleaved: split a tile's (row lane, component) units across its k
+// parts so neighbouring threads take one node's neighbouring values (1), or
+// give part j component j of every row lane (0).
+#ifndef OGS_KI_SPLIT
+#define OGS_KI_SPLIT 1
+#endif
 
 template <typename T>
 __device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem) {
@@ -56,39 +62,40 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// Entry e of this lane lives at stage[e * 32 + lane].
+// `lane` picks the tile rows (rows lane, lane + 32, ...); entry e of the
+// thread lives at stage[e * 32 + slot], slot = the thread's own lane.
 template <typename T, int MODE, int D>
 __device__ __forceinline__ void async_issue_vals(const WarpState& s, const T* src, const T* gv, int64_t stride, int K,
-                                                 int k, bool gmask, int lane, T* stage) {
+                                                 int k, bool gmask, int lane, int slot, T* stage) {
   constexpr int RPT = warp_rows_per_lane(D);
 #pragma unroll
   for (int j = 0; j < RPT; ++j) {
     if (j * 32 + lane < s.cnt) {
       if (MODE == kModeScatter) {
-        cp_async_elem(stage + j * 32 + lane, gv + static_cast<int64_t>(s.R[j]) * K + k);
+        cp_async_elem(stage + j * 32 + slot, gv + static_cast<int64_t>(s.R[j]) * K + k);
       } else {
 #pragma unroll
         for (int q = 0; q < D; ++q)
           if (!gmask || ((s.emask >> (j * D + q)) & 1u))
-            cp_async_elem(stage + (j * D + q) * 32 + lane, src + static_cast<int64_t>(s.I[j * D + q]) * stride);
+            cp_async_elem(stage + (j * D + q) * 32 + slot, src + static_cast<int64_t>(s.I[j * D + q]) * stride);
       }
     }
   }
 }
 
 template <typename T, int MODE, int D>
-__device__ __forceinline__ void async_read_vals(const WarpState& s, bool gmask, int lane, const T* stage,
+__device__ __forceinline__ void async_read_vals(const WarpState& s, bool gmask, int lane, int slot, const T* stage,
                                                 T (&V)[kWarpSlots]) {
   constexpr int RPT = warp_rows_per_lane(D);
 #pragma unroll
   for (int j = 0; j < RPT; ++j) {
     if (j * 32 + lane < s.cnt) {
       if (MODE == kModeScatter) {
-        V[j] = stage[j * 32 + lane];
+        V[j] = stage[j * 32 + slot];
       } else {
 #pragma unroll
         for (int q = 0; q < D; ++q)
-          if (!gmask || ((s.emask >> (j * D + q)) & 1u)) V[j * D + q] = stage[(j * D + q) * 32 + lane];
+          if (!gmask || ((s.emask >> (j * D + q)) & 1u)) V[j * D + q] = stage[(j * D + q) * 32 + slot];
       }
     }
   }
@@ -116,14 +123,19 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
   const int64_t nitems = nw * K;
   const int64_t wid = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + warp;
   // Warp w takes items w, w+W, w+2W, ...: the grid sweeps the mesh front to
-  // back.  k > 1 interleaved: item = (tile, component), tile-major, so the k
-  // warps of one tile run side by side and share the sectors of each node's
-  // k values; separate arrays: item = (array, tile), array-major, so one
-  // array and the column ids stay in L2 while the grid sweeps it.  (A warp
-  // running a contiguous run of (tile, component) items, loading each tile's
-  // column ids once, was measured much slower: 83 vs 62 us for k = 3 on 3.5 M
-  // permuted nodes.)  Items are followed as (tile, component) pairs, advanced
-  // by W without division.
+  // back.  k > 1 interleaved: item = (tile, part), tile-major, parts 0..k-1.
+  // A tile's 32 row lanes times k components are 32k (row lane, component)
+  // units, and part j takes units 32j .. 32j+31: thread t of part j works row
+  // lane (32j+t) / k, component (32j+t) % k.  Neighbouring threads then read
+  // the k neighbouring values of one node in the same instruction, so a
+  // gather touches the sectors of about 32/k nodes instead of 32 (with OGS_KI_SPLIT
+  // = 0, part j is component j for all 32 row lanes, and the k warps of a
+  // tile meet each node's sectors only through L1).  Separate arrays: item =
+  // (array, tile), array-major, so one array and the column ids stay in L2
+  // while the grid sweeps it.  (A warp running a contiguous run of (tile,
+  // component) items, loading each tile's column ids once, was measured much
+  // slower: 83 vs 62 us for k = 3 on 3.5 M permuted nodes.)  Items are
+  // followed as (tile, part) pairs, advanced by W without division.
   const int64_t i0 = wid;
   if (i0 >= nitems) return;
   int64_t i = i0;
@@ -157,6 +169,24 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
     }
   };
   T* gv = static_cast<T*>(f.gv);
+  // The thread's row lane and component in item part c, recomputed where
+  // needed rather than carried through the pipeline (registers).  Division by
+  // k as a multiply-high by ceil(2^32 / k), exact while (32k) * k < 2^32.
+  const bool split = KL == kKInterleaved && OGS_KI_SPLIT;
+  const uint32_t kmagic = split && K > 1 ? 0xFFFFFFFFu / static_cast<uint32_t>(K) + 1u : 0u;
+  const bool kmagic_ok = K < 11585;
+  auto unit = [&](int c, int& rl, int& comp) {
+    if (split) {
+      const uint32_t u = static_cast<uint32_t>(c) * 32u + static_cast<uint32_t>(lane);
+      rl = static_cast<int>(kmagic_ok ? __umulhi(u, kmagic) : u / static_cast<uint32_t>(K));
+      comp = static_cast<int>(u) - rl * K;
+    } else {
+      rl = lane;
+      comp = c;
+    }
+  };
+  int rcur, kcur;
+  unit(ccur, rcur, kcur);
 
   // prologue: the descriptors of items i, i+1 step, i+2 steps in one round
   // trip, the column ids of the first two in the next, then the gathers of
@@ -174,18 +204,20 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
     }
   }
   WarpState scur, snxt;
-#define OGS_A_LOAD(D, TILE, TI, S) warp_load_state<MODE, D>(m.b[D], TILE, m.wemask, TI, use_mask, pat, lane, S)
-#define OGS_A_LOAD_CUR(D) OGS_A_LOAD(D, cur, tcur, scur)
+#define OGS_A_LOAD(D, TILE, TI, RL, S) warp_load_state<MODE, D>(m.b[D], TILE, m.wemask, TI, use_mask, pat, RL, S)
+#define OGS_A_LOAD_CUR(D) OGS_A_LOAD(D, cur, tcur, rcur, scur)
   OGS_DEGREE_SWITCH(cur.bucket, OGS_A_LOAD_CUR)
 #undef OGS_A_LOAD_CUR
   if (has1) {
-#define OGS_A_LOAD_NXT(D) OGS_A_LOAD(D, nxt, tnxt, snxt)
+    int rnxt, knxt;
+    unit(cnxt, rnxt, knxt);
+#define OGS_A_LOAD_NXT(D) OGS_A_LOAD(D, nxt, tnxt, rnxt, snxt)
     OGS_DEGREE_SWITCH(nxt.bucket, OGS_A_LOAD_NXT)
 #undef OGS_A_LOAD_NXT
   }
   {
-    const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, ccur);
-#define OGS_A_ISSUE0(D) async_issue_vals<T, MODE, D>(scur, src, gv, stride, K, ccur, gmask, lane, ring)
+    const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, kcur);
+#define OGS_A_ISSUE0(D) async_issue_vals<T, MODE, D>(scur, src, gv, stride, K, kcur, gmask, rcur, lane, ring)
     OGS_DEGREE_SWITCH(cur.bucket, OGS_A_ISSUE0)
 #undef OGS_A_ISSUE0
   }
@@ -197,9 +229,11 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
     const bool more2 = i + 2 * step < iend;
     const int nstage = stage == kAsyncStages - 1 ? 0 : stage + 1;
     if (more1) {
-      const T* src1 = (MODE == kModeScatter) ? nullptr : field_base<T>(f, cnxt);
+      int rnxt, knxt;
+      unit(cnxt, rnxt, knxt);
+      const T* src1 = (MODE == kModeScatter) ? nullptr : field_base<T>(f, knxt);
       T* st1 = ring + nstage * (kWarpSlots * 32);
-#define OGS_A_ISSUE1(D) async_issue_vals<T, MODE, D>(snxt, src1, gv, stride, K, cnxt, gmask, lane, st1)
+#define OGS_A_ISSUE1(D) async_issue_vals<T, MODE, D>(snxt, src1, gv, stride, K, knxt, gmask, rnxt, lane, st1)
       OGS_DEGREE_SWITCH(nxt.bucket, OGS_A_ISSUE1)
 #undef OGS_A_ISSUE1
     }
@@ -208,7 +242,9 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
     Tile n3{};
     int tn3 = 0, cn3 = 0;
     if (more2) {
-#define OGS_A_LOAD_NN(D) OGS_A_LOAD(D, nn, tnn, snn)
+      int rnn, knn;
+      unit(cnn, rnn, knn);
+#define OGS_A_LOAD_NN(D) OGS_A_LOAD(D, nn, tnn, rnn, snn)
       OGS_DEGREE_SWITCH(nn.bucket, OGS_A_LOAD_NN)
 #undef OGS_A_LOAD_NN
       if (i + 3 * step < iend) {
@@ -218,13 +254,14 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_async_kernel(const 
     }
     cp_async_wait<1>();  // the gathers of item i are in
     {
-      T* dst = (MODE == kModeGather) ? nullptr : field_base<T>(f, ccur);
+      unit(ccur, rcur, kcur);
+      T* dst = (MODE == kModeGather) ? nullptr : field_base<T>(f, kcur);
       const T* st0 = ring + stage * (kWarpSlots * 32);
       T V[kWarpSlots];
 #define OGS_A_FOLD(D)                                                                              \
   do {                                                                                             \
-    async_read_vals<T, MODE, D>(scur, gmask, lane, st0, V);                                        \
-    warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, ccur, gmask, smode, gslib, lane, V); \
+    async_read_vals<T, MODE, D>(scur, gmask, rcur, lane, st0, V);                                  \
+    warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, kcur, gmask, smode, gslib, rcur, V); \
   } while (0)
       OGS_DEGREE_SWITCH(cur.bucket, OGS_A_FOLD)
 #undef OGS_A_FOLD

@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(kBlock, OCC)
     const BatchEntry& be = E[cur.e];
     const T* src = static_cast<const T*>(be.v) + cur.k;
     const bool gmask = be.gather_n != 0;
-#define OGS_BA_ISSUE0(D) async_issue_vals<T, kModeGS, D>(scur, src, nullptr, be.K, be.K, cur.k, gmask, lane, ring)
+#define OGS_BA_ISSUE0(D) async_issue_vals<T, kModeGS, D>(scur, src, nullptr, be.K, be.K, cur.k, gmask, lane, lane, ring)
     OGS_DEGREE_SWITCH(cur.d, OGS_BA_ISSUE0)
 #undef OGS_BA_ISSUE0
   }
@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(kBlock, OCC)
       const T* src1 = static_cast<const T*>(be.v) + nxt.k;
       const bool gmask1 = be.gather_n != 0;
       T* st1 = ring + nstage * (kWarpSlots * 32);
-#define OGS_BA_ISSUE1(D) async_issue_vals<T, kModeGS, D>(snxt, src1, nullptr, be.K, be.K, nxt.k, gmask1, lane, st1)
+#define OGS_BA_ISSUE1(D) async_issue_vals<T, kModeGS, D>(snxt, src1, nullptr, be.K, be.K, nxt.k, gmask1, lane, lane, st1)
       OGS_DEGREE_SWITCH(nxt.d, OGS_BA_ISSUE1)
 #undef OGS_BA_ISSUE1
     }
@@ -321,7 +321,7 @@ __global__ void __launch_bounds__(kBlock, OCC)
       T V[kWarpSlots];
 #define OGS_BA_FOLD(D)                                                            \
   do {                                                                            \
-    async_read_vals<T, kModeGS, D>(scur, gmask, lane, st0, V);                    \
+    async_read_vals<T, kModeGS, D>(scur, gmask, lane, lane, st0, V);              \
     fold_store_rt<T, D>(op, scur, dst, K, K, cur.k, gmask, smode, lane, V);       \
   } while (0)
       OGS_DEGREE_SWITCH(cur.d, OGS_BA_FOLD)

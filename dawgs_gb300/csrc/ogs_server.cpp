@@ -61,14 +61,33 @@ constexpr int kAdmitWindow = 64;
 constexpr int kMaxPassOvers = 16;
 // Fields up to this size go to the small lane.
 constexpr size_t kSmallBytes = size_t(4) << 20;
-// Launches a lane keeps on the GPU at once.  While they run, newly admitted
-// requests wait in the lane and go together in its next launch: under load
-// the batches grow and the per-launch costs are shared; with nothing running
-// a request is launched at once.
-#ifndef OGS_SERVER_LANE_LAUNCHES
-#define OGS_SERVER_LANE_LAUNCHES 2
+// Turns (batched launches with their copies) a lane keeps on the GPU at once.
+// While they run, newly admitted requests wait in the lane and go together in
+// its next turn: under load the batches grow and the per-launch costs are
+// shared; with nothing running a request is launched at once.
+#ifndef OGS_SERVER_SMALL_TURNS
+#define OGS_SERVER_SMALL_TURNS 2
 #endif
-static_assert(OGS_SERVER_LANE_LAUNCHES >= 1 && OGS_SERVER_LANE_LAUNCHES < 8, "a lane rotates 8 turn events");
+#ifndef OGS_SERVER_LARGE_TURNS
+#define OGS_SERVER_LARGE_TURNS 4
+#endif
+static_assert(OGS_SERVER_SMALL_TURNS >= 1 && OGS_SERVER_SMALL_TURNS < 8, "a lane rotates 8 turn events");
+static_assert(OGS_SERVER_LARGE_TURNS >= 1 && OGS_SERVER_LARGE_TURNS < 8, "a lane rotates 8 turn events");
+// Field bytes one turn copies in (at least one request).  Both lanes share
+// the copy engines: a large-lane turn of many fields would hold a small
+// request's copies back for milliseconds, so large-lane turns are short and
+// more of them are kept in flight to keep the copies streaming.
+#ifndef OGS_SERVER_SMALL_TURN_BYTES
+#define OGS_SERVER_SMALL_TURN_BYTES (size_t(64) << 20)
+#endif
+#ifndef OGS_SERVER_LARGE_TURN_BYTES
+#define OGS_SERVER_LARGE_TURN_BYTES (size_t(16) << 20)
+#endif
+// Copies longer than this are issued in pieces of this size (0: whole), so
+// the other lane's copies can go between them.
+#ifndef OGS_SERVER_COPY_CHUNK
+#define OGS_SERVER_COPY_CHUNK 0
+#endif
 // Launch tables per server (shared by both lanes), and completion events made
 // at creation (more are made when requests in flight need them).
 constexpr int kTableSlots = 64;
@@ -147,7 +166,20 @@ struct Lane {
   std::deque<cudaEvent_t> running;  // its turns' launches not yet finished, in order (worker only)
   cudaEvent_t turn_done[8] = {};     // recorded after each turn's launches, used in rotation
   int next_turn_event = 0;
+  int max_turns = 1;       // turns kept in flight
+  size_t turn_bytes = 0;   // field bytes one turn copies in (at least one request)
 };
+
+// One copy, in pieces of OGS_SERVER_COPY_CHUNK bytes when that is set.
+int copy_async(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind, cudaStream_t st) {
+  const size_t piece = OGS_SERVER_COPY_CHUNK ? size_t(OGS_SERVER_COPY_CHUNK) : bytes;
+  for (size_t at = 0; at < bytes; at += piece) {
+    const size_t len = std::min(piece, bytes - at);
+    const int e = cudaMemcpyAsync(static_cast<char*>(dst) + at, static_cast<const char*>(src) + at, len, kind, st);
+    if (e) return e;
+  }
+  return 0;
+}
 
 }  // namespace
 }  // namespace ogsgb
@@ -271,7 +303,7 @@ int launch_group(ogs_server_s* s, Lane& lane, TableSlot& slot, const std::vector
   for (int i = 0; !e && i < n; ++i) {
     Req* q = grp[i];
     q->t_launch = t;
-    e = cudaMemcpyAsync(q->r.host, s->pool_base + q->off, q->bytes, cudaMemcpyDeviceToHost, lane.out);
+    e = copy_async(q->r.host, s->pool_base + q->off, q->bytes, cudaMemcpyDeviceToHost, lane.out);
     if (!e && s->spare_events.empty()) {
       cudaEvent_t ev = nullptr;
       e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
@@ -297,18 +329,25 @@ int launch_lane(ogs_server_s* s, Lane& lane) {
     if (q == cudaErrorNotReady) break;
     lane.running.pop_front();
   }
-  if (static_cast<int>(lane.running.size()) >= OGS_SERVER_LANE_LAUNCHES) return 0;  // next turn, a larger batch
+  if (static_cast<int>(lane.running.size()) >= lane.max_turns) return 0;  // next turn, a larger batch
+  // this turn: the oldest ready requests up to the turn's byte budget
+  size_t take = 0, bytes = 0;
+  while (take < lane.ready.size() && (take == 0 || bytes + lane.ready[take]->bytes <= lane.turn_bytes))
+    bytes += lane.ready[take++]->bytes;
   std::vector<Req*> grp[4];
   int groups = 0;
-  for (Req* q : lane.ready) {
+  for (size_t j = 0; j < take; ++j) {
+    Req* q = lane.ready[j];
     if (grp[q->r.type].empty()) groups++;
     grp[q->r.type].push_back(q);
   }
   std::vector<TableSlot*> slots = free_slots(s, groups);
   if (static_cast<int>(slots.size()) < groups) return 0;  // next turn
   int e = 0;
-  for (Req* q : lane.ready)
-    if (!e) e = cudaMemcpyAsync(s->pool_base + q->off, q->r.host, q->bytes, cudaMemcpyHostToDevice, lane.in);
+  for (size_t j = 0; j < take; ++j) {
+    Req* q = lane.ready[j];
+    if (!e) e = copy_async(s->pool_base + q->off, q->r.host, q->bytes, cudaMemcpyHostToDevice, lane.in);
+  }
   if (!e) e = cudaEventRecord(lane.copied, lane.in);
   int j = 0;
   for (int type = OGS_FLOAT; !e && type <= OGS_INT64; ++type)
@@ -319,7 +358,7 @@ int launch_lane(ogs_server_s* s, Lane& lane) {
     e = cudaEventRecord(ev, lane.compute);
     if (!e) lane.running.push_back(ev);
   }
-  lane.ready.clear();
+  lane.ready.erase(lane.ready.begin(), lane.ready.begin() + static_cast<std::ptrdiff_t>(take));
   return e;
 }
 
@@ -486,6 +525,10 @@ ogs_status ogs_server_create(ogs_server* out, const ogs_server_config* cfg) {
   cudaError_t e = cudaGetDevice(&s->device);
   if (e == cudaSuccess) e = dev_malloc(&s->pool_base, static_cast<size_t>(cfg->field_budget_bytes));
   if (e == cudaSuccess) s->pool.reset(static_cast<size_t>(cfg->field_budget_bytes));
+  s->lanes[0].max_turns = OGS_SERVER_SMALL_TURNS;
+  s->lanes[0].turn_bytes = OGS_SERVER_SMALL_TURN_BYTES;
+  s->lanes[1].max_turns = OGS_SERVER_LARGE_TURNS;
+  s->lanes[1].turn_bytes = OGS_SERVER_LARGE_TURN_BYTES;
   for (Lane& l : s->lanes) {
     for (cudaStream_t* st : {&l.in, &l.compute, &l.out})
       if (e == cudaSuccess) e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking);

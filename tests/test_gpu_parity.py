@@ -112,6 +112,41 @@ def test_many_layout_matches_per_array_oracle(cuda, oracle_mod, dtype, nf):
             assert same_bits(from_dev(dx), want)
 
 
+@pytest.mark.parametrize("k", [2, 3, 5, 7, 8, 13, 33])
+def test_interleaved_k_every_mode(cuda, oracle_mod, k):
+    """Interleaved k > 1: a tile's 32 row lanes x k components are split over
+    its k warp items, so a thread's row lane and component depend on k (powers
+    of two and not, k > 32).  GatherScatter on Unsigned and Signed handles
+    (every transpose), Gather and Scatter on a Signed unique handle."""
+    base = mesh.permute_elements(mesh.box_ids(6, 5, 4, 3), 3, seed=11)
+    for kind in ("unsigned", "signed"):
+        ids = base if kind == "unsigned" else signed_ids(base, seed=12)
+        g = ogs.ogs_t().Setup(ids.size, ids.copy(), None, ogs.Signed if kind == "signed" else ogs.Unsigned)
+        ref = oracle_mod.OracleOgs(ids.copy(), kind)
+        for dtype, op in ((np.float64, "add"), (np.int32, "max"), (np.float32, "mul")):
+            for trans in TRANS:
+                v = values(k * ids.size, dtype, op, seed=40 + k)
+                d = to_dev(v)
+                g.GatherScatter(d, k, ogs.Op[op.capitalize()], ogs.Transpose[
+                    {"sym": "Sym", "notrans": "NoTrans", "trans": "Trans"}[trans]])
+                want = ref.gather_scatter(v.copy(), k, op, trans)
+                assert same_bits(from_dev(d), want), (kind, dtype, op, trans, first_diff(from_dev(d), want))
+    ids_a, ids_b = base.copy(), base.copy()
+    g = ogs.ogs_t().Setup(ids_a.size, ids_a, None, ogs.Signed, ogs.Auto, True)
+    ref = oracle_mod.OracleOgs(ids_b, "signed", unique=True)
+    v = values(k * base.size, np.float64, "add", seed=60 + k)
+    for trans, T in (("trans", ogs.Trans), ("notrans", ogs.NoTrans)):
+        want = np.zeros(k * g.Ngather, np.float64)
+        ref.gather(want, v, k, "add", trans)
+        dgv = torch.zeros(k * g.Ngather, dtype=torch.float64, device="cuda")
+        g.Gather(dgv, to_dev(v), k, ogs.Add, T)
+        assert same_bits(from_dev(dgv), want), ("gather", trans)
+        v0 = values(k * base.size, np.float64, "add", seed=61 + k)
+        dv = to_dev(v0)
+        g.Scatter(dv, to_dev(want), k, T)
+        assert same_bits(from_dev(dv), ref.scatter(v0.copy(), want, k, trans)), ("scatter", trans)
+
+
 def test_c3_irregular_multifield(cuda, oracle_mod):
     """32x32x16 p=5 with a seeded element permutation; k=3 interleaved and k=8
     separate arrays; fp64/fp32 Add (U[-1,1]) and Mul (U[0.5,2])."""
