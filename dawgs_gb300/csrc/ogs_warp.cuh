@@ -119,6 +119,8 @@ __device__ __forceinline__ void warp_fold_store(const WarpState& s, T* dst, T* g
 #pragma unroll
         for (int q = 1; q < D; ++q)
           if (!gmask || ((s.emask >> (j * D + q)) & 1u)) op_apply<T, OP>(a, V[j * D + q]);
+      } else if ((OP == OGS_ADD || OP == OGS_MUL) && !gmask) {
+        a = fold_from_first<T, OP, D>(V, j * D);
       } else {
         a = op_init<T, OP>();
 #pragma unroll
