@@ -387,7 +387,9 @@ def run_served(a, dev, L, stream):
     Requests are admitted against a 16 GB device budget.  First a saturation
     run (all requests queued at once) gives the throughput; then Poisson
     arrivals at 25%, 50% and 80% of it give p50/p99 latency, counted from each
-    request's scheduled arrival.  The whole arrival schedule is handed to the
+    request's scheduled arrival, after 0.5 s of the same arrival stream that
+    is served but not counted (a GPU and host coming out of idle run the
+    first tens of milliseconds slower).  The whole arrival schedule is handed to the
     server at once, which admits each request at its arrival time, so the
     client's own submission cost does not stand in for the server's.  Plain =
     the same requests one after another through ogs_gather_scatter_host."""
@@ -433,6 +435,8 @@ def run_served(a, dev, L, stream):
         req_table[i] = _lib.OgsServerRequest(int(meshes[i]), 1 if dts[i] == 0 else 0, int(ks[i]), int(ops[i]), 0,
                                              0, views[i].data_ptr())
 
+    warm_s = 0.5
+
     def serve(rate):
         srv = ogs.ogs_server_t(field_budget_bytes=16 << 30, max_inflight=4096, max_batch=256)
         for g in handles:
@@ -440,19 +444,30 @@ def run_served(a, dev, L, stream):
         # the first arrival comes after the whole schedule has been handed
         # over (queueing 100k requests takes some ms, under the server's lock)
         t0 = srv.clock() + 0.25
+        nw = 0
         if rate is None:
             arr = np.full(n, t0)
+            table = req_table
         else:
-            gaps = -np.log(1.0 - (mesh.splitmix64(np.arange(n, dtype=np.uint64) + np.uint64(99)) >> np.uint64(11))
-                           .astype(np.float64) / 9007199254740992.0) / rate
+            # Poisson arrivals, led by warm_s seconds of the same stream that
+            # are served but not counted: an idle GPU and host start slower
+            # (clocks and power states ramp up), which a server under steady
+            # load does not see
+            nw = int(warm_s * rate)
+            gaps = -np.log(1.0 - (mesh.splitmix64(np.arange(nw + n, dtype=np.uint64) + np.uint64(99))
+                                  >> np.uint64(11)).astype(np.float64) / 9007199254740992.0) / rate
             arr = t0 + np.cumsum(gaps)
+            table = (_lib.OgsServerRequest * (nw + n))()
+            C.memmove(table, req_table, C.sizeof(_lib.OgsServerRequest) * nw)
+            C.memmove(C.addressof(table) + C.sizeof(_lib.OgsServerRequest) * nw, req_table,
+                      C.sizeof(_lib.OgsServerRequest) * n)
         # the whole arrival schedule is handed over at once: the server admits
         # each request at its arrival time, and latency counts from there
         arr = np.ascontiguousarray(arr, dtype=np.float64)
         first = C.c_int64()
-        _lib.check(L.ogs_server_submit_many(srv._s, req_table, arr.ctypes.data, n, C.byref(first)))
+        _lib.check(L.ogs_server_submit_many(srv._s, table, arr.ctypes.data, nw + n, C.byref(first)))
         srv.drain()
-        ta, tl, td = srv.times(0, n, launched=True)
+        ta, tl, td = srv.times(first.value + nw, n, launched=True)
         launches, _ = srv.counters()
         worker = srv.stats()
         srv.Free()
@@ -461,6 +476,8 @@ def run_served(a, dev, L, stream):
         out = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                "p999_ms": float(np.percentile(lat, 99.9)),
                "dofs_per_s": dofs / span, "requests_per_s": n / span, "launches": int(launches)}
+        if nw:
+            out["warm_up"] = {"requests": nw, "seconds": warm_s, "counted": False}
         # when the slow requests arrived (50 ms bins from the first arrival)
         # and whether the worker itself stalled: a tail made of a few bins, at
         # a regular period, with long gaps between the worker's passes or

@@ -42,6 +42,10 @@ constexpr int kAsyncStages = OGS_ASYNC_STAGES;
 // k > 1 interleaved: split a tile's (row lane, component) units across its k
 // parts so neighbouring threads take one node's neighbouring values (1), or
 // give part j component j of every row lane (0).
+// Resident CTAs per SM of the grid (0: as many as fit).
+#ifndef OGS_ASYNC_CTAS
+#define OGS_ASYNC_CTAS 0
+#endif
 #ifndef OGS_KI_SPLIT
 #define OGS_KI_SPLIT 1
 #endif
@@ -299,6 +303,9 @@ inline int async_grid(int64_t nitems) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_async_kernel<T, OP, MODE, KL, PLAIN>, kBlock,
                                                   async_smem_bytes<T>());
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+#if OGS_ASYNC_CTAS > 0
+    if (bps > OGS_ASYNC_CTAS) bps = OGS_ASYNC_CTAS;
+#endif
     return (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1);
   });
   const int64_t need = (nitems + (kBlock / 32) - 1) / (kBlock / 32);

@@ -265,6 +265,7 @@ ogs_status ogs_batch_create(ogs_batch* out, int type, const ogs_batch_entry* ent
     be.wemask = e.h->dmaps.wemask;
     be.v = e.d_v;
     be.K = e.k;
+    be.kmagic = batch_kmagic(e.k);
     be.op = e.op;
     fill_pattern(e.h, e.trans, be);
     b->host_entries.push_back(be);

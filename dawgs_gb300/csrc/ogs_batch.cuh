@@ -44,17 +44,35 @@ __device__ __forceinline__ int batch_entry_of(const int64_t* starts, int n, int6
   return lo;
 }
 
-// One work item, (entry e, warp record r, component k), reduced to what the
-// fold needs: field, masks, column ids of the record's bucket and its tile.
+// A thread's (row lane, component) in part `part` of an entry's record: as
+// in the single-mesh kernel, a record's 32 row lanes x K components are split
+// over its K items, so neighbouring threads read neighbouring components of
+// one node.
+__device__ __forceinline__ void batch_unit(int K, uint32_t kmagic, int part, int lane, int& rl, int& comp) {
+  if (K == 1) {
+    rl = lane;
+    comp = 0;
+    return;
+  }
+  const uint32_t u = static_cast<uint32_t>(part) * 32u + static_cast<uint32_t>(lane);
+  rl = static_cast<int>(kmagic ? __umulhi(u, kmagic) : u / static_cast<uint32_t>(K));
+  comp = static_cast<int>(u) - rl * K;
+}
+
+// One work item, (entry e, warp record r, part), reduced to what the fold
+// needs: field, masks, column ids of the record's bucket and its tile, and
+// the thread's component k and row lane.
 struct BatchItem {
   const WarpRec* recs;
   const int32_t* cols;
   void* v;
   const uint8_t* wemask;
-  int32_t K, flags;  // flags: op | gather_n << 4 | scatter_n << 5 | limit_n << 6 | use_mask << 7
+  int32_t K, flags;  // flags: op | gather_n << 4 | scatter_n << 5 | limit_n << 6 | use_mask << 7 | row lane << 8
   int32_t e, r, k;
   int32_t begin, bucket_count, stride, nP;
 };
+
+__device__ __forceinline__ int item_lane(const BatchItem& it) { return (it.flags >> 8) & 31; }
 
 __device__ __forceinline__ void batch_load_entry(const BatchEntry* E, int e, BatchItem& it) {
   const BatchEntry& be = E[e];
@@ -77,16 +95,20 @@ __device__ __forceinline__ void batch_load_rec(BatchItem& it) {
 
 // The item at global index i: its entry by binary search over the prefix,
 // then its record and component.
-__device__ __forceinline__ void batch_item_at(const BatchEntry* E, const int64_t* st, int n, int64_t i,
+__device__ __forceinline__ void batch_item_at(const BatchEntry* E, const int64_t* st, int n, int64_t i, int lane,
                                               BatchItem& it) {
   batch_load_entry(E, batch_entry_of(st, n, i), it);
-  const int64_t local = i - st[it.e];
-  it.r = static_cast<int32_t>(local / it.K);
-  it.k = static_cast<int32_t>(local - static_cast<int64_t>(it.r) * it.K);
+  const int32_t local = static_cast<int32_t>(i - st[it.e]);  // items of one entry fit 32 bits
+  it.r = local / it.K;
+  int rl, comp;
+  batch_unit(it.K, E[it.e].kmagic, local - it.r * it.K, lane, rl, comp);
+  it.k = comp;
+  it.flags |= rl << 8;
   batch_load_rec(it);
 }
 
-__device__ __forceinline__ void batch_load_state(const BatchItem& it, int lane, WarpState& s) {
+__device__ __forceinline__ void batch_load_state(const BatchItem& it, WarpState& s) {
+  const int lane = item_lane(it);
   const Pattern pat{(it.flags >> 4) & 1, (it.flags >> 5) & 1, (it.flags >> 6) & 1};
   DevBucket b;
   b.cols = it.cols;
@@ -130,28 +152,28 @@ __global__ void __launch_bounds__(BLOCK, OCC * 256 / BLOCK)
   if (i >= nitems) return;
 
   BatchItem cur, nxt;
-  batch_item_at(E, st, n, i, cur);
+  batch_item_at(E, st, n, i, lane, cur);
   WarpState scur;
-  batch_load_state(cur, lane, scur);
-  if (i + W < nitems) batch_item_at(E, st, n, i + W, nxt);
+  batch_load_state(cur, scur);
+  if (i + W < nitems) batch_item_at(E, st, n, i + W, lane, nxt);
 
   for (;;) {
     const bool more = i + W < nitems;
-    const int K = cur.K, k = cur.k, d = cur.bucket_count >> 16;
+    const int K = cur.K, k = cur.k, d = cur.bucket_count >> 16, rl = item_lane(cur);
     const bool gmask = (cur.flags >> 4) & 1;
     const int smode = (cur.flags >> 5) & 1;
     T* base = static_cast<T*>(cur.v) + k;
     T V[kWarpSlots];
-#define OGS_B_VALS(D) warp_load_vals<T, kModeGS, D>(scur, base, nullptr, K, K, k, gmask, lane, V)
+#define OGS_B_VALS(D) warp_load_vals<T, kModeGS, D>(scur, base, nullptr, K, K, k, gmask, rl, V)
     OGS_DEGREE_SWITCH(d, OGS_B_VALS)
 #undef OGS_B_VALS
     WarpState snxt;
     BatchItem nn;
     if (more) {
-      batch_load_state(nxt, lane, snxt);
-      if (i + 2 * W < nitems) batch_item_at(E, st, n, i + 2 * W, nn);
+      batch_load_state(nxt, snxt);
+      if (i + 2 * W < nitems) batch_item_at(E, st, n, i + 2 * W, lane, nn);
     }
-#define OGS_B_FOLD(D) fold_store_rt<T, D>(cur.flags & 15, scur, base, K, K, k, gmask, smode, lane, V)
+#define OGS_B_FOLD(D) fold_store_rt<T, D>(cur.flags & 15, scur, base, K, K, k, gmask, smode, rl, V)
     OGS_DEGREE_SWITCH(d, OGS_B_FOLD)
 #undef OGS_B_FOLD
     if (!more) break;
@@ -202,22 +224,28 @@ inline int launch_batch_shape(const BatchEntry* E, const int64_t* starts, int n,
 // record, component, degree -- and its field, op and record are read again
 // from the entry table and the record (L1-resident) where they are needed.
 struct BatchPos {
-  int32_t e, r, k, d;
+  int32_t e, r, k, d;  // k: the thread's component; d: degree | row lane << 8
 };
 
-__device__ __forceinline__ BatchPos batch_pos(const BatchEntry* E, const int64_t* st, int n, int64_t i) {
+__device__ __forceinline__ int pos_deg(const BatchPos& p) { return p.d & 0xFF; }
+__device__ __forceinline__ int pos_lane(const BatchPos& p) { return p.d >> 8; }
+
+__device__ __forceinline__ BatchPos batch_pos(const BatchEntry* E, const int64_t* st, int n, int64_t i, int lane) {
   BatchPos p;
   p.e = batch_entry_of(st, n, i);
   const int K = E[p.e].K;
   const int32_t local = static_cast<int32_t>(i - st[p.e]);  // items of one entry fit 32 bits
   p.r = local / K;
-  p.k = local - p.r * K;
-  p.d = E[p.e].recs[p.r].bucket_count >> 16;
+  int rl, comp;
+  batch_unit(K, E[p.e].kmagic, local - p.r * K, lane, rl, comp);
+  p.k = comp;
+  p.d = (E[p.e].recs[p.r].bucket_count >> 16) | (rl << 8);
   return p;
 }
 
 template <int D>
-__device__ __forceinline__ void batch_state_at(const BatchEntry* E, const BatchPos& p, int lane, WarpState& s) {
+__device__ __forceinline__ void batch_state_at(const BatchEntry* E, const BatchPos& p, WarpState& s) {
+  const int lane = pos_lane(p);
   const BatchEntry& be = E[p.e];
   const WarpRec& w = be.recs[p.r];
   DevBucket b;
@@ -262,26 +290,27 @@ __global__ void __launch_bounds__(kBlock, OCC)
   int64_t i = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + warp;
   if (i >= nitems) return;
 
-  BatchPos cur = batch_pos(E, st, n, i), nxt{}, nn{};
+  BatchPos cur = batch_pos(E, st, n, i, lane), nxt{}, nn{};
   const bool has1 = i + W < nitems;
-  if (has1) nxt = batch_pos(E, st, n, i + W);
-  if (i + 2 * W < nitems) nn = batch_pos(E, st, n, i + 2 * W);
+  if (has1) nxt = batch_pos(E, st, n, i + W, lane);
+  if (i + 2 * W < nitems) nn = batch_pos(E, st, n, i + 2 * W, lane);
   WarpState scur, snxt;
-#define OGS_BA_STATE(D, P, S) batch_state_at<D>(E, P, lane, S)
+#define OGS_BA_STATE(D, P, S) batch_state_at<D>(E, P, S)
 #define OGS_BA_CUR(D) OGS_BA_STATE(D, cur, scur)
-  OGS_DEGREE_SWITCH(cur.d, OGS_BA_CUR)
+  OGS_DEGREE_SWITCH(pos_deg(cur), OGS_BA_CUR)
 #undef OGS_BA_CUR
   if (has1) {
 #define OGS_BA_NXT(D) OGS_BA_STATE(D, nxt, snxt)
-    OGS_DEGREE_SWITCH(nxt.d, OGS_BA_NXT)
+    OGS_DEGREE_SWITCH(pos_deg(nxt), OGS_BA_NXT)
 #undef OGS_BA_NXT
   }
   {
     const BatchEntry& be = E[cur.e];
     const T* src = static_cast<const T*>(be.v) + cur.k;
     const bool gmask = be.gather_n != 0;
-#define OGS_BA_ISSUE0(D) async_issue_vals<T, kModeGS, D>(scur, src, nullptr, be.K, be.K, cur.k, gmask, lane, lane, ring)
-    OGS_DEGREE_SWITCH(cur.d, OGS_BA_ISSUE0)
+#define OGS_BA_ISSUE0(D) \
+  async_issue_vals<T, kModeGS, D>(scur, src, nullptr, be.K, be.K, cur.k, gmask, pos_lane(cur), lane, ring)
+    OGS_DEGREE_SWITCH(pos_deg(cur), OGS_BA_ISSUE0)
 #undef OGS_BA_ISSUE0
   }
   cp_async_commit();
@@ -296,8 +325,9 @@ __global__ void __launch_bounds__(kBlock, OCC)
       const T* src1 = static_cast<const T*>(be.v) + nxt.k;
       const bool gmask1 = be.gather_n != 0;
       T* st1 = ring + nstage * (kWarpSlots * 32);
-#define OGS_BA_ISSUE1(D) async_issue_vals<T, kModeGS, D>(snxt, src1, nullptr, be.K, be.K, nxt.k, gmask1, lane, lane, st1)
-      OGS_DEGREE_SWITCH(nxt.d, OGS_BA_ISSUE1)
+#define OGS_BA_ISSUE1(D) \
+  async_issue_vals<T, kModeGS, D>(snxt, src1, nullptr, be.K, be.K, nxt.k, gmask1, pos_lane(nxt), lane, st1)
+      OGS_DEGREE_SWITCH(pos_deg(nxt), OGS_BA_ISSUE1)
 #undef OGS_BA_ISSUE1
     }
     cp_async_commit();
@@ -305,9 +335,9 @@ __global__ void __launch_bounds__(kBlock, OCC)
     BatchPos n3{};
     if (more2) {
 #define OGS_BA_NN(D) OGS_BA_STATE(D, nn, snn)
-      OGS_DEGREE_SWITCH(nn.d, OGS_BA_NN)
+      OGS_DEGREE_SWITCH(pos_deg(nn), OGS_BA_NN)
 #undef OGS_BA_NN
-      if (i + 3 * W < nitems) n3 = batch_pos(E, st, n, i + 3 * W);
+      if (i + 3 * W < nitems) n3 = batch_pos(E, st, n, i + 3 * W, lane);
     }
     cp_async_wait<1>();  // the gathers of item i are in
     {
@@ -321,10 +351,10 @@ __global__ void __launch_bounds__(kBlock, OCC)
       T V[kWarpSlots];
 #define OGS_BA_FOLD(D)                                                            \
   do {                                                                            \
-    async_read_vals<T, kModeGS, D>(scur, gmask, lane, lane, st0, V);              \
-    fold_store_rt<T, D>(op, scur, dst, K, K, cur.k, gmask, smode, lane, V);       \
+    async_read_vals<T, kModeGS, D>(scur, gmask, pos_lane(cur), lane, st0, V);     \
+    fold_store_rt<T, D>(op, scur, dst, K, K, cur.k, gmask, smode, pos_lane(cur), V); \
   } while (0)
-      OGS_DEGREE_SWITCH(cur.d, OGS_BA_FOLD)
+      OGS_DEGREE_SWITCH(pos_deg(cur), OGS_BA_FOLD)
 #undef OGS_BA_FOLD
     }
     if (!more1) break;

@@ -154,7 +154,12 @@ struct BatchEntry {
   void* v;                 // field, K interleaved components per node
   int32_t K, op;
   int32_t gather_n, scatter_n, limit_n, use_mask;
+  uint32_t kmagic;         // ceil(2^32 / K) for 1 < K < 11585 (division by K as a multiply-high), else 0
+  int32_t reserved;
 };
+// The multiply-high divisor of a batch entry's K: floor(u / K) ==
+// umulhi(u, ceil(2^32 / K)) for every u < 32 K when (32 K) K < 2^32.
+inline uint32_t batch_kmagic(int K) { return K > 1 && K < 11585 ? 0xFFFFFFFFu / static_cast<uint32_t>(K) + 1u : 0u; }
 // Work items of a batched launch: each (warp record, component) pair of each
 // entry; starts[e] = first item of entry e, records of an entry in order with
 // their K components adjacent.

@@ -275,6 +275,7 @@ int launch_group(ogs_server_s* s, Lane& lane, TableSlot& slot, const std::vector
     e.wemask = h->dmaps.wemask;
     e.v = s->pool_base + q->off;
     e.K = q->r.k;
+    e.kmagic = batch_kmagic(q->r.k);
     e.op = q->r.op;
     const Pattern p = pattern_for(h, kModeGS, q->r.trans);
     e.gather_n = p.gather_n;
@@ -624,6 +625,8 @@ ogs_status ogs_server_submit_many(ogs_server s, const ogs_server_request* rs, co
       const size_t nn = static_cast<size_t>(s->meshes[r->mesh]->N);
       if (nn > 0 && node_bytes > static_cast<size_t>(s->cfg.field_budget_bytes) / nn)
         return set_error(OGS_ERANGE, std::string(fn) + ": the field is larger than the whole budget");
+      if (static_cast<int64_t>(s->meshes[r->mesh]->dmaps.nwtiles) * r->k > INT32_MAX)
+        return set_error(OGS_ERANGE, std::string(fn) + ": more than 2^31 work items in one request");
     }
     try {
       s->all.reserve(s->all.size() + static_cast<size_t>(n));

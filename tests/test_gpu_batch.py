@@ -16,7 +16,7 @@ OPN = {ogs.Add: "add", ogs.Mul: "mul", ogs.Max: "max", ogs.Min: "min"}
 TRN = {ogs.Sym: "sym", ogs.NoTrans: "notrans", ogs.Trans: "trans"}
 
 
-def build_mix(oracle_mod, count, seed, dtype, signed=False, general=False):
+def build_mix(oracle_mod, count, seed, dtype, signed=False, general=False, ks=(1, 2, 3, 4)):
     out = []
     for j, (nx, ny, nz, p) in enumerate(mesh.mesh_mix(count, seed, lo=1, hi=6, pmax=5)):
         ids = mesh.box_ids(nx, ny, nz, p)
@@ -28,7 +28,7 @@ def build_mix(oracle_mod, count, seed, dtype, signed=False, general=False):
             kind = ogs.Signed
         g = ogs.ogs_t().Setup(ids.size, ids.copy(), None, kind)
         ref = oracle_mod.OracleOgs(ids.copy(), "signed" if kind == ogs.Signed else "unsigned")
-        k = 1 + (j % 4)
+        k = ks[j % len(ks)]
         op = OPS[j % 4]
         trans = [ogs.Sym, ogs.NoTrans, ogs.Trans][j % 3] if kind == ogs.Signed else ogs.Sym
         v = values(k * ids.size, dtype, OPN[op], seed=100 + j)
@@ -112,3 +112,20 @@ def test_batch_configurations_give_the_same_results(cuda, oracle_mod, cfg):
         b.GatherScatter()
         torch.cuda.synchronize()
         check(mix, fields)
+
+
+@pytest.mark.parametrize("cfg", [dict(), dict(occupancy=3, ctas_per_sm=3), dict(pipeline=1),
+                                 dict(pipeline=1, occupancy=3, ctas_per_sm=2)],
+                         ids=["register", "register-occ3", "ring", "ring-occ3"])
+@pytest.mark.parametrize("dtype", [np.float64, np.int32], ids=lambda t: np.dtype(t).name)
+def test_batch_larger_k(cuda, oracle_mod, cfg, dtype):
+    """Entries with k = 5, 7, 13 and 33 beside k = 1 and 2: each record's 32
+    row lanes x k components are split over its k items, by the entry's
+    multiply-high divisor (k < 11585) in both pipelines."""
+    mix = build_mix(oracle_mod, 12, seed=17, dtype=dtype, signed=True, ks=(5, 1, 7, 13, 2, 33))
+    fields = [torch.from_numpy(v.copy()).cuda() for (_, _, v, _, _, _) in mix]
+    b = ogs.ogs_batch_t([(g, d, k, op, trans) for (g, _, _, k, op, trans), d in zip(mix, fields)])
+    b.set_config(**cfg)
+    b.GatherScatter()
+    torch.cuda.synchronize()
+    check(mix, fields)
