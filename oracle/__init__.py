@@ -3,7 +3,10 @@
 TEST INFRASTRUCTURE ONLY.  ``OracleOgs`` wraps oracle/ogs_oracle.c, the C
 restatement of libParanumal's host ogs (libs/ogs/ogsSetup.cpp,
 libs/ogs/ogsOperator.cpp); ``GsRef`` wraps gslib built from the reference tree
-(oracle/_ref/libgsref.so, present only where the reference sources are).  Only
+(oracle/_ref/libgsref.so) and ``RefOperator`` the reference's own host
+operator, libs/ogs/ogsOperator.cpp compiled unmodified against stand-ins for
+OCCA and MPI (oracle/_ref/libogsref.so); both exist only where the reference
+sources are.  Only
 tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import this
 module; the dawgs_gb300 package never does.
 """
@@ -18,6 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libogs_oracle.so")
 GSREF_SO = os.path.join(HERE, "_ref", "libgsref.so")
+OGSREF_SO = os.path.join(HERE, "_ref", "libogsref.so")
 
 
 def gslib_src() -> str | None:
@@ -31,6 +35,20 @@ def gslib_src() -> str | None:
         except (OSError, subprocess.CalledProcessError):
             return None
     return src if src and os.path.isdir(src) else None
+
+
+def ref_root() -> str | None:
+    """The reference tree: $REF_ROOT, else the build recipe's default; None
+    when its host operator source is absent."""
+    root = os.environ.get("REF_ROOT")
+    if not root:
+        try:
+            root = subprocess.run(["make", "-s", "-C", HERE, "print-ref-root"], check=True,
+                                  capture_output=True, text=True).stdout.strip()
+        except (OSError, subprocess.CalledProcessError):
+            return None
+    ok = root and os.path.isfile(os.path.join(root, "libs", "ogs", "ogsOperator.cpp"))
+    return root if ok else None
 
 TYPES = {"float32": 0, "float64": 1, "int32": 2, "int64": 3}
 NP_OF = {0: np.float32, 1: np.float64, 2: np.int32, 3: np.int64}
@@ -47,6 +65,9 @@ def build(ref: bool | None = None) -> None:
         raise FileNotFoundError("gslib sources not found: set GSLIB_SRC to the reference's 3rdParty/gslib/src")
     if src is not None:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"GSLIB_SRC={src}"], check=True)
+    root = ref_root() if ref is not False else None
+    if root is not None:
+        subprocess.run(["make", "-s", "-C", HERE, "refop", f"REF_ROOT={root}"], check=True)
 
 
 _lib = None
@@ -91,6 +112,63 @@ def gslib():
         L.gsref_free.argtypes = [C.c_void_p]
         _gs = L
     return _gs
+
+
+def ogsref_available() -> bool:
+    return os.path.exists(OGSREF_SO)
+
+
+_ogsref = None
+
+
+def ogsref():
+    global _ogsref
+    if _ogsref is None:
+        L = C.CDLL(OGSREF_SO)
+        L.ogsref_create.restype = C.c_void_p
+        L.ogsref_create.argtypes = [C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                    C.c_void_p]
+        L.ogsref_free.argtypes = [C.c_void_p]
+        L.ogsref_gather_scatter.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int,
+                                            C.c_int]
+        L.ogsref_gather.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int, C.c_int,
+                                    C.c_int, C.c_int]
+        L.ogsref_scatter.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int, C.c_int,
+                                     C.c_int]
+        _ogsref = L
+    return _ogsref
+
+
+class RefOperator:
+    """The reference's own host ogs operator (ogsOperator_t, ogsOperator.cpp)
+    over the maps of an ``OracleOgs`` handle: its GatherScatter, Gather and
+    Scatter run the reference's code on those maps."""
+
+    def __init__(self, o: "OracleOgs"):
+        self._maps = o.maps()
+        rsT, ciT, rsN, ciN = self._maps
+        self.Ngather = o.Ngather
+        self._h = ogsref().ogsref_create(o.N, o.NlocalT, _ptr(rsT), _ptr(ciT), o.NlocalP, _ptr(rsN), _ptr(ciN))
+
+    def __del__(self):
+        if _ogsref is not None and getattr(self, "_h", None):
+            _ogsref.ogsref_free(self._h)
+            self._h = None
+
+    def gather_scatter(self, v: np.ndarray, k: int, op="add", trans="sym"):
+        ogsref().ogsref_gather_scatter(self._h, _ptr(v), v.size, TYPES[v.dtype.name], k, _code(OPS, op),
+                                       _code(TRANS, trans))
+        return v
+
+    def gather(self, gv: np.ndarray, v: np.ndarray, k: int, op="add", trans="trans"):
+        ogsref().ogsref_gather(self._h, _ptr(gv), gv.size, _ptr(v), v.size, TYPES[v.dtype.name], k,
+                               _code(OPS, op), _code(TRANS, trans))
+        return gv
+
+    def scatter(self, v: np.ndarray, gv: np.ndarray, k: int, trans="notrans"):
+        ogsref().ogsref_scatter(self._h, _ptr(v), v.size, _ptr(gv), gv.size, TYPES[v.dtype.name], k,
+                                _code(TRANS, trans))
+        return v
 
 
 def _code(table, x):
