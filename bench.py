@@ -457,10 +457,16 @@ def run_served(a, dev, L, stream):
             gaps = -np.log(1.0 - (mesh.splitmix64(np.arange(nw + n, dtype=np.uint64) + np.uint64(99))
                                   >> np.uint64(11)).astype(np.float64) / 9007199254740992.0) / rate
             arr = t0 + np.cumsum(gaps)
+            # the warm-up requests repeat the table from its start (as often
+            # as the warm-up needs), then the counted requests follow
             table = (_lib.OgsServerRequest * (nw + n))()
-            C.memmove(table, req_table, C.sizeof(_lib.OgsServerRequest) * nw)
-            C.memmove(C.addressof(table) + C.sizeof(_lib.OgsServerRequest) * nw, req_table,
-                      C.sizeof(_lib.OgsServerRequest) * n)
+            rsz = C.sizeof(_lib.OgsServerRequest)
+            done = 0
+            while done < nw:
+                m = min(n, nw - done)
+                C.memmove(C.addressof(table) + rsz * done, req_table, rsz * m)
+                done += m
+            C.memmove(C.addressof(table) + rsz * nw, req_table, rsz * n)
         # the whole arrival schedule is handed over at once: the server admits
         # each request at its arrival time, and latency counts from there
         arr = np.ascontiguousarray(arr, dtype=np.float64)

@@ -31,6 +31,7 @@ struct ogs_batch_s {
   unsigned flags = 0;
   std::vector<ogs_batch_entry> entries;
   std::vector<ogsgb::BatchEntry> host_entries;  // every entry, field and pattern filled in
+  int plain = 1;  // no entry has N masks, a store mode or a row limit
   std::vector<int64_t> items;                   // per entry: warp records x k
   ogs_batch_config cfg{};
   // derived from cfg
@@ -159,13 +160,13 @@ int launch_all(ogs_batch_s* b, const BatchEntry* fields, cudaStream_t st) {
     const int grid = b->cfg.ctas_per_sm > 0 ? b->cfg.ctas_per_sm * std::max(1, b->cfg.sms) : 0;
     switch (b->type) {
       case OGS_FLOAT: e = launch_batch_f32(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy,
-                                             b->cfg.pipeline, st); break;
+                                             b->cfg.pipeline, b->plain, st); break;
       case OGS_DOUBLE: e = launch_batch_f64(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy,
-                                             b->cfg.pipeline, st); break;
+                                             b->cfg.pipeline, b->plain, st); break;
       case OGS_INT32: e = launch_batch_i32(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy,
-                                             b->cfg.pipeline, st); break;
+                                             b->cfg.pipeline, b->plain, st); break;
       default: e = launch_batch_i64(b->d_entries, b->d_starts, n, nitems, grid, b->cfg.block, b->cfg.occupancy,
-                                             b->cfg.pipeline, st); break;
+                                             b->cfg.pipeline, b->plain, st); break;
     }
     for (size_t q = 0; !e && q < b->general.size(); ++q) {
       const int i = b->general[q];
@@ -269,6 +270,7 @@ ogs_status ogs_batch_create(ogs_batch* out, int type, const ogs_batch_entry* ent
     be.op = e.op;
     fill_pattern(e.h, e.trans, be);
     b->host_entries.push_back(be);
+    if (!batch_plain(be)) b->plain = 0;
     b->items.push_back(static_cast<int64_t>(e.h->dmaps.nwtiles) * e.k);
   }
   int sms = 1;

@@ -107,9 +107,10 @@ __device__ __forceinline__ void batch_item_at(const BatchEntry* E, const int64_t
   batch_load_rec(it);
 }
 
+template <bool PLAIN>
 __device__ __forceinline__ void batch_load_state(const BatchItem& it, WarpState& s) {
   const int lane = item_lane(it);
-  const Pattern pat{(it.flags >> 4) & 1, (it.flags >> 5) & 1, (it.flags >> 6) & 1};
+  const Pattern pat = PLAIN ? Pattern{0, 0, 0} : Pattern{(it.flags >> 4) & 1, (it.flags >> 5) & 1, (it.flags >> 6) & 1};
   DevBucket b;
   b.cols = it.cols;
   b.rows = nullptr;
@@ -124,7 +125,7 @@ __device__ __forceinline__ void batch_load_state(const BatchItem& it, WarpState&
   t.begin = it.begin;
   t.count = it.bucket_count & 0xFFFF;
   t.first_row = 0;
-  const bool use_mask = (it.flags >> 7) & 1;
+  const bool use_mask = !PLAIN && ((it.flags >> 7) & 1);
 #define OGS_B_LOAD(D) t.bucket = D; warp_load_state<kModeGS, D>(b, t, it.wemask, it.r, use_mask, pat, lane, s)
   OGS_DEGREE_SWITCH(it.bucket_count >> 16, OGS_B_LOAD)
 #undef OGS_B_LOAD
@@ -136,7 +137,9 @@ __device__ __forceinline__ void batch_load_state(const BatchItem& it, WarpState&
 // sectors through L1/L2 (a warp walking a contiguous run of items was much
 // slower on large meshes, as for the single-mesh kernel).  The prefix
 // `starts` is staged in shared memory (dynamic, (n+1) entries) when it fits.
-template <typename T, int BLOCK, int OCC>
+// PLAIN: every entry folds and stores every member (no N masks, no limit on
+// the rows): the mask and store-mode branches drop out at compile time.
+template <typename T, int BLOCK, int OCC, bool PLAIN>
 __global__ void __launch_bounds__(BLOCK, OCC * 256 / BLOCK)
     ogs_batch_kernel(const BatchEntry* __restrict__ E, const int64_t* __restrict__ starts, int n) {
   extern __shared__ int64_t s_starts[];
@@ -154,14 +157,14 @@ __global__ void __launch_bounds__(BLOCK, OCC * 256 / BLOCK)
   BatchItem cur, nxt;
   batch_item_at(E, st, n, i, lane, cur);
   WarpState scur;
-  batch_load_state(cur, scur);
+  batch_load_state<PLAIN>(cur, scur);
   if (i + W < nitems) batch_item_at(E, st, n, i + W, lane, nxt);
 
   for (;;) {
     const bool more = i + W < nitems;
     const int K = cur.K, k = cur.k, d = cur.bucket_count >> 16, rl = item_lane(cur);
-    const bool gmask = (cur.flags >> 4) & 1;
-    const int smode = (cur.flags >> 5) & 1;
+    const bool gmask = !PLAIN && ((cur.flags >> 4) & 1);
+    const int smode = PLAIN ? 0 : (cur.flags >> 5) & 1;
     T* base = static_cast<T*>(cur.v) + k;
     T V[kWarpSlots];
 #define OGS_B_VALS(D) warp_load_vals<T, kModeGS, D>(scur, base, nullptr, K, K, k, gmask, rl, V)
@@ -170,7 +173,7 @@ __global__ void __launch_bounds__(BLOCK, OCC * 256 / BLOCK)
     WarpState snxt;
     BatchItem nn;
     if (more) {
-      batch_load_state(nxt, snxt);
+      batch_load_state<PLAIN>(nxt, snxt);
       if (i + 2 * W < nitems) batch_item_at(E, st, n, i + 2 * W, lane, nn);
     }
 #define OGS_B_FOLD(D) fold_store_rt<T, D>(cur.flags & 15, scur, base, K, K, k, gmask, smode, rl, V)
@@ -184,7 +187,7 @@ __global__ void __launch_bounds__(BLOCK, OCC * 256 / BLOCK)
   }
 }
 
-template <typename T, int BLOCK, int OCC>
+template <typename T, int BLOCK, int OCC, bool PLAIN>
 inline int batch_blocks_per_sm(int* sms) {
   static DeviceCache bps_cache, sms_cache;
   int dev = 0;
@@ -197,23 +200,23 @@ inline int batch_blocks_per_sm(int* sms) {
   // occupancy with the largest starts table (the registers decide it)
   return bps_cache.get(dev, [] {
     int bps = 0;
-    cudaFuncSetAttribute(ogs_batch_kernel<T, BLOCK, OCC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(ogs_batch_kernel<T, BLOCK, OCC, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>((kBatchSmem + 1) * sizeof(int64_t)));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_batch_kernel<T, BLOCK, OCC>, BLOCK, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_batch_kernel<T, BLOCK, OCC, PLAIN>, BLOCK, 0);
     return bps > 0 ? bps : 1;
   });
 }
 
-template <typename T, int BLOCK, int OCC>
+template <typename T, int BLOCK, int OCC, bool PLAIN>
 inline int launch_batch_shape(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid,
                               cudaStream_t st) {
   int sms = 0;
-  const int bps = batch_blocks_per_sm<T, BLOCK, OCC>(&sms);
+  const int bps = batch_blocks_per_sm<T, BLOCK, OCC, PLAIN>(&sms);
   int64_t g = grid > 0 ? grid : static_cast<int64_t>(bps) * sms;
   const int64_t need = (nitems + (BLOCK / 32) - 1) / (BLOCK / 32);
   if (g > need) g = need;
   const size_t smem = n <= kBatchSmem ? static_cast<size_t>(n + 1) * sizeof(int64_t) : 0;
-  ogs_batch_kernel<T, BLOCK, OCC><<<static_cast<unsigned>(g), BLOCK, smem, st>>>(E, starts, n);
+  ogs_batch_kernel<T, BLOCK, OCC, PLAIN><<<static_cast<unsigned>(g), BLOCK, smem, st>>>(E, starts, n);
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -243,7 +246,7 @@ __device__ __forceinline__ BatchPos batch_pos(const BatchEntry* E, const int64_t
   return p;
 }
 
-template <int D>
+template <int D, bool PLAIN>
 __device__ __forceinline__ void batch_state_at(const BatchEntry* E, const BatchPos& p, WarpState& s) {
   const int lane = pos_lane(p);
   const BatchEntry& be = E[p.e];
@@ -263,8 +266,8 @@ __device__ __forceinline__ void batch_state_at(const BatchEntry* E, const BatchP
   t.begin = w.begin;
   t.count = w.bucket_count & 0xFFFF;
   t.first_row = 0;
-  const Pattern pat{be.gather_n, be.scatter_n, be.limit_n};
-  warp_load_state<kModeGS, D>(b, t, be.wemask, p.r, be.use_mask != 0, pat, lane, s);
+  const Pattern pat = PLAIN ? Pattern{0, 0, 0} : Pattern{be.gather_n, be.scatter_n, be.limit_n};
+  warp_load_state<kModeGS, D>(b, t, be.wemask, p.r, !PLAIN && be.use_mask != 0, pat, lane, s);
 }
 
 template <typename T>
@@ -272,7 +275,7 @@ OGS_HD constexpr size_t batch_ring_bytes() {  // 8 warps x 2 stages x kWarpSlots
   return static_cast<size_t>(kBlock / 32) * kAsyncStages * kWarpSlots * 32 * sizeof(T);
 }
 
-template <typename T, int OCC>
+template <typename T, int OCC, bool PLAIN>
 __global__ void __launch_bounds__(kBlock, OCC)
     ogs_batch_async_kernel(const BatchEntry* __restrict__ E, const int64_t* __restrict__ starts, int n) {
   extern __shared__ __align__(16) unsigned char batch_smem[];
@@ -295,7 +298,7 @@ __global__ void __launch_bounds__(kBlock, OCC)
   if (has1) nxt = batch_pos(E, st, n, i + W, lane);
   if (i + 2 * W < nitems) nn = batch_pos(E, st, n, i + 2 * W, lane);
   WarpState scur, snxt;
-#define OGS_BA_STATE(D, P, S) batch_state_at<D>(E, P, S)
+#define OGS_BA_STATE(D, P, S) batch_state_at<D, PLAIN>(E, P, S)
 #define OGS_BA_CUR(D) OGS_BA_STATE(D, cur, scur)
   OGS_DEGREE_SWITCH(pos_deg(cur), OGS_BA_CUR)
 #undef OGS_BA_CUR
@@ -307,7 +310,7 @@ __global__ void __launch_bounds__(kBlock, OCC)
   {
     const BatchEntry& be = E[cur.e];
     const T* src = static_cast<const T*>(be.v) + cur.k;
-    const bool gmask = be.gather_n != 0;
+    const bool gmask = !PLAIN && be.gather_n != 0;
 #define OGS_BA_ISSUE0(D) \
   async_issue_vals<T, kModeGS, D>(scur, src, nullptr, be.K, be.K, cur.k, gmask, pos_lane(cur), lane, ring)
     OGS_DEGREE_SWITCH(pos_deg(cur), OGS_BA_ISSUE0)
@@ -323,7 +326,7 @@ __global__ void __launch_bounds__(kBlock, OCC)
     if (more1) {
       const BatchEntry& be = E[nxt.e];
       const T* src1 = static_cast<const T*>(be.v) + nxt.k;
-      const bool gmask1 = be.gather_n != 0;
+      const bool gmask1 = !PLAIN && be.gather_n != 0;
       T* st1 = ring + nstage * (kWarpSlots * 32);
 #define OGS_BA_ISSUE1(D) \
   async_issue_vals<T, kModeGS, D>(snxt, src1, nullptr, be.K, be.K, nxt.k, gmask1, pos_lane(nxt), lane, st1)
@@ -344,8 +347,8 @@ __global__ void __launch_bounds__(kBlock, OCC)
       const BatchEntry& be = E[cur.e];
       const int K = be.K;
       T* dst = static_cast<T*>(be.v) + cur.k;
-      const bool gmask = be.gather_n != 0;
-      const int smode = be.scatter_n;
+      const bool gmask = !PLAIN && be.gather_n != 0;
+      const int smode = PLAIN ? 0 : be.scatter_n;
       const int op = be.op;
       const T* st0 = ring + stage * (kWarpSlots * 32);
       T V[kWarpSlots];
@@ -370,7 +373,7 @@ __global__ void __launch_bounds__(kBlock, OCC)
 #undef OGS_BA_STATE
 }
 
-template <typename T, int OCC>
+template <typename T, int OCC, bool PLAIN>
 inline int batch_async_blocks_per_sm(int* sms) {
   static DeviceCache bps_cache, sms_cache;
   int dev = 0;
@@ -383,24 +386,24 @@ inline int batch_async_blocks_per_sm(int* sms) {
   return bps_cache.get(dev, [] {
     int bps = 0;
     const size_t smem = batch_ring_bytes<T>() + (kBatchSmem + 1) * sizeof(int64_t);
-    cudaFuncSetAttribute(ogs_batch_async_kernel<T, OCC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(ogs_batch_async_kernel<T, OCC, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          static_cast<int>(smem));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_batch_async_kernel<T, OCC>, kBlock,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_batch_async_kernel<T, OCC, PLAIN>, kBlock,
                                                   batch_ring_bytes<T>() + 257 * sizeof(int64_t));
     return bps > 0 ? bps : 1;
   });
 }
 
-template <typename T, int OCC>
+template <typename T, int OCC, bool PLAIN>
 inline int launch_batch_async_shape(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid,
                                     cudaStream_t st) {
   int sms = 0;
-  const int bps = batch_async_blocks_per_sm<T, OCC>(&sms);
+  const int bps = batch_async_blocks_per_sm<T, OCC, PLAIN>(&sms);
   int64_t g = grid > 0 ? grid : static_cast<int64_t>(bps) * sms;
   const int64_t need = (nitems + (kBlock / 32) - 1) / (kBlock / 32);
   if (g > need) g = need;
   const size_t smem = batch_ring_bytes<T>() + (n <= kBatchSmem ? static_cast<size_t>(n + 1) * sizeof(int64_t) : 0);
-  ogs_batch_async_kernel<T, OCC><<<static_cast<unsigned>(g), kBlock, smem, st>>>(E, starts, n);
+  ogs_batch_async_kernel<T, OCC, PLAIN><<<static_cast<unsigned>(g), kBlock, smem, st>>>(E, starts, n);
   return static_cast<int>(cudaGetLastError());
 }
 
@@ -409,9 +412,11 @@ inline int launch_batch_async_shape(const BatchEntry* E, const int64_t* starts, 
 template <typename T, int BLOCK, int OCC>
 inline int preload_batch_shape() {
   cudaFuncAttributes a;
-  const cudaError_t e = cudaFuncGetAttributes(&a, ogs_batch_kernel<T, BLOCK, OCC>);
+  cudaError_t e = cudaFuncGetAttributes(&a, ogs_batch_kernel<T, BLOCK, OCC, true>);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&a, ogs_batch_kernel<T, BLOCK, OCC, false>);
   int sms = 0;
-  if (e == cudaSuccess) batch_blocks_per_sm<T, BLOCK, OCC>(&sms);
+  if (e == cudaSuccess) batch_blocks_per_sm<T, BLOCK, OCC, true>(&sms);
+  if (e == cudaSuccess) batch_blocks_per_sm<T, BLOCK, OCC, false>(&sms);
   return static_cast<int>(e);
 }
 
@@ -419,19 +424,27 @@ inline int preload_batch_shape() {
 // 128 or 256 threads per CTA; occ: the register budget, 2 or 3 256-thread
 // CTAs per SM; pipe 0: the register pipeline, 1: the cp.async ring.
 // pipe 1: the cp.async ring (256-thread blocks; occ 2 or 3).
+template <typename T, bool PLAIN>
+inline int launch_batch_plain(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
+                              int occ, int pipe, cudaStream_t st) {
+  if (pipe == 1)
+    return occ == 3 ? launch_batch_async_shape<T, 3, PLAIN>(E, starts, n, nitems, grid, st)
+                    : launch_batch_async_shape<T, 2, PLAIN>(E, starts, n, nitems, grid, st);
+  if (block == 128)
+    return occ == 3 ? launch_batch_shape<T, 128, 3, PLAIN>(E, starts, n, nitems, grid, st)
+                    : launch_batch_shape<T, 128, 2, PLAIN>(E, starts, n, nitems, grid, st);
+  return occ == 3 ? launch_batch_shape<T, 256, 3, PLAIN>(E, starts, n, nitems, grid, st)
+                  : launch_batch_shape<T, 256, 2, PLAIN>(E, starts, n, nitems, grid, st);
+}
+
+// plain: every entry has the plain pattern (Sym or no masks; see ogs_batch_kernel).
 template <typename T>
 inline int launch_batch_typed(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid,
-                              int block, int occ, int pipe, void* stream) {
+                              int block, int occ, int pipe, int plain, void* stream) {
   if (nitems <= 0) return 0;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (pipe == 1)
-    return occ == 3 ? launch_batch_async_shape<T, 3>(E, starts, n, nitems, grid, st)
-                    : launch_batch_async_shape<T, 2>(E, starts, n, nitems, grid, st);
-  if (block == 128)
-    return occ == 3 ? launch_batch_shape<T, 128, 3>(E, starts, n, nitems, grid, st)
-                    : launch_batch_shape<T, 128, 2>(E, starts, n, nitems, grid, st);
-  return occ == 3 ? launch_batch_shape<T, 256, 3>(E, starts, n, nitems, grid, st)
-                  : launch_batch_shape<T, 256, 2>(E, starts, n, nitems, grid, st);
+  return plain ? launch_batch_plain<T, true>(E, starts, n, nitems, grid, block, occ, pipe, st)
+               : launch_batch_plain<T, false>(E, starts, n, nitems, grid, block, occ, pipe, st);
 }
 
 }  // namespace ogsgb

@@ -159,6 +159,9 @@ struct BatchEntry {
 };
 // The multiply-high divisor of a batch entry's K: floor(u / K) ==
 // umulhi(u, ceil(2^32 / K)) for every u < 32 K when (32 K) K < 2^32.
+inline bool batch_plain(const BatchEntry& e) {
+  return !e.gather_n && !e.scatter_n && !e.limit_n && !e.use_mask;
+}
 inline uint32_t batch_kmagic(int K) { return K > 1 && K < 11585 ? 0xFFFFFFFFu / static_cast<uint32_t>(K) + 1u : 0u; }
 // Work items of a batched launch: each (warp record, component) pair of each
 // entry; starts[e] = first item of entry e, records of an entry in order with
@@ -303,15 +306,17 @@ int launch_i64(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern p
 
 // Batched launch over `n` entries (ogs_batch.cuh); grid <= 0 = one full wave;
 // block = 128 or 256 threads per CTA; occ = 2 or 3 (register budget: 256-thread
-// CTAs per SM); pipe = 0 register pipeline, 1 cp.async ring (256 threads).
+// CTAs per SM); pipe = 0 register pipeline, 1 cp.async ring (256 threads);
+// plain = 1 when no entry has N masks, a store mode or a row limit
+// (batch_plain), which selects kernels without those branches.
 int launch_batch_f32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     int occ, int pipe, void* stream);
+                     int occ, int pipe, int plain, void* stream);
 int launch_batch_f64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     int occ, int pipe, void* stream);
+                     int occ, int pipe, int plain, void* stream);
 int launch_batch_i32(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     int occ, int pipe, void* stream);
+                     int occ, int pipe, int plain, void* stream);
 int launch_batch_i64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     int occ, int pipe, void* stream);
+                     int occ, int pipe, int plain, void* stream);
 
 // Device and page-locked host allocations (ogs_alloc.cpp): counted, and made
 // to fail on demand by ogs_debug_fail_alloc.  Every allocation of the library

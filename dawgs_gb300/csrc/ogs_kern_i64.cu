@@ -8,8 +8,9 @@ int launch_i64(const DevMaps& m, const FieldArgs& f, int mode, int op, Pattern p
   return launch_typed<int64_t>(m, f, mode, op, pat, stream);
 }
 int launch_batch_i64(const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int grid, int block,
-                     int occ, int pipe, void* stream) {
-  return launch_batch_typed<int64_t>(E, starts, n, nitems, grid, block, occ, pipe, stream);
-}int preload_batch_i64() { return preload_batch_shape<int64_t, 256, 2>(); }
+                     int occ, int pipe, int plain, void* stream) {
+  return launch_batch_typed<int64_t>(E, starts, n, nitems, grid, block, occ, pipe, plain, stream);
+}
+int preload_batch_i64() { return preload_batch_shape<int64_t, 256, 2>(); }
 
 }  // namespace ogsgb

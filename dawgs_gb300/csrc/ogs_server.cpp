@@ -15,12 +15,13 @@
 //              itself until it fits (no starvation);
 //   launch  -- admitted requests go to one of two lanes by size (small fields
 //              and large fields), each with its own copy-in, compute and
-//              copy-out streams: a small request never waits behind a large
-//              request's copies.  Everything admitted to a lane since its last
-//              turn is copied in and run as one batched launch per value type
-//              (ogs_batch.cuh).  A launch needs a table slot whose previous
-//              launch is over; when none is free the lane waits for the next
-//              turn instead of blocking the worker.
+//              copy-out streams.  A lane's turn copies in its oldest ready
+//              requests up to the lane's byte budget and runs them as one
+//              batched launch per value type (ogs_batch.cuh); the lanes share
+//              the copy engines, so the budgets keep a large-lane turn from
+//              holding a small request's copies back.  A launch needs a table
+//              slot whose previous launch is over; when none is free the lane
+//              waits for the next turn instead of blocking the worker.
 // Requests arriving while others are on the GPU are admitted and launched on
 // the next turn, so their copies and kernels overlap the earlier ones'.
 // Latency is completion minus arrival: the submit time, or the arrival time
@@ -214,12 +215,13 @@ struct ogs_server_s {
 namespace ogsgb {
 namespace {
 
-int batch_launch(int type, const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, cudaStream_t st) {
+int batch_launch(int type, const BatchEntry* E, const int64_t* starts, int n, int64_t nitems, int plain,
+                 cudaStream_t st) {
   switch (type) {
-    case OGS_FLOAT: return launch_batch_f32(E, starts, n, nitems, 0, 256, 2, 0, st);
-    case OGS_DOUBLE: return launch_batch_f64(E, starts, n, nitems, 0, 256, 2, 0, st);
-    case OGS_INT32: return launch_batch_i32(E, starts, n, nitems, 0, 256, 2, 0, st);
-    default: return launch_batch_i64(E, starts, n, nitems, 0, 256, 2, 0, st);
+    case OGS_FLOAT: return launch_batch_f32(E, starts, n, nitems, 0, 256, 2, 0, plain, st);
+    case OGS_DOUBLE: return launch_batch_f64(E, starts, n, nitems, 0, 256, 2, 0, plain, st);
+    case OGS_INT32: return launch_batch_i32(E, starts, n, nitems, 0, 256, 2, 0, plain, st);
+    default: return launch_batch_i64(E, starts, n, nitems, 0, 256, 2, 0, plain, st);
   }
 }
 
@@ -266,6 +268,7 @@ std::vector<TableSlot*> free_slots(ogs_server_s* s, int want) {
 int launch_group(ogs_server_s* s, Lane& lane, TableSlot& slot, const std::vector<Req*>& grp, int type) {
   const int n = static_cast<int>(grp.size());
   slot.h_starts[0] = 0;
+  int plain = 1;
   for (int i = 0; i < n; ++i) {
     const Req* q = grp[i];
     const ogs_handle_s* h = s->meshes[q->r.mesh];
@@ -282,13 +285,14 @@ int launch_group(ogs_server_s* s, Lane& lane, TableSlot& slot, const std::vector
     e.scatter_n = p.scatter_n;
     e.limit_n = p.limit_n;
     e.use_mask = (e.gather_n || e.scatter_n) && h->kind == OGS_SIGNED;
+    if (!batch_plain(e)) plain = 0;
     slot.h_starts[i + 1] = slot.h_starts[i] + static_cast<int64_t>(h->dmaps.nwtiles) * q->r.k;
   }
   cudaStream_t st = lane.compute;
   int e = cudaMemcpyAsync(slot.d_entries, slot.h_entries, sizeof(BatchEntry) * n, cudaMemcpyHostToDevice, st);
   if (!e) e = cudaMemcpyAsync(slot.d_starts, slot.h_starts, sizeof(int64_t) * (n + 1), cudaMemcpyHostToDevice, st);
   if (!e) e = cudaStreamWaitEvent(st, lane.copied, 0);
-  if (!e) e = batch_launch(type, slot.d_entries, slot.d_starts, n, slot.h_starts[n], st);
+  if (!e) e = batch_launch(type, slot.d_entries, slot.d_starts, n, slot.h_starts[n], plain, st);
   for (int i = 0; !e && i < n; ++i) {
     const Req* q = grp[i];
     const ogs_handle_s* h = s->meshes[q->r.mesh];

@@ -95,11 +95,14 @@ def test_batch_of_one_equals_plain_call(cuda, oracle_mod):
                                  dict(pipeline=1), dict(pipeline=1, occupancy=3, ctas_per_sm=2),
                                  dict(solo_items=1, solo_streams=3), dict(solo_items=40, solo_streams=8, ctas_per_sm=1)],
                          ids=["default", "block128", "occ3", "block128-occ3", "ring", "ring-occ3", "all-solo", "mixed"])
-def test_batch_configurations_give_the_same_results(cuda, oracle_mod, cfg):
+@pytest.mark.parametrize("signed", [True, False], ids=["masked", "plain"])
+def test_batch_configurations_give_the_same_results(cuda, oracle_mod, cfg, signed):
     """Every configuration the tuner may choose -- block size, CTAs per SM,
     entries run alone on the single-mesh kernel over parallel graph branches
-    -- gives each entry the oracle's result."""
-    mix = build_mix(oracle_mod, 30, seed=13, dtype=np.float64, signed=True, general=True)
+    -- gives each entry the oracle's result, for a batch with Signed entries
+    (masks and store modes) and for an all-Sym Unsigned batch (the kernels
+    built without those branches)."""
+    mix = build_mix(oracle_mod, 30, seed=13, dtype=np.float64, signed=signed, general=True)
     fields = [torch.from_numpy(v.copy()).cuda() for (_, _, v, _, _, _) in mix]
     b = ogs.ogs_batch_t([(g, d, k, op, trans) for (g, _, _, k, op, trans), d in zip(mix, fields)], graph=True)
     b.set_config(**cfg)
