@@ -131,6 +131,9 @@ def ogsref():
         L.ogsref_free.argtypes = [C.c_void_p]
         L.ogsref_gather_scatter.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int,
                                             C.c_int]
+        L.ogsref_time_gather_scatter.restype = C.c_double
+        L.ogsref_time_gather_scatter.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int, C.c_int,
+                                                 C.c_int, C.c_int, C.c_int]
         L.ogsref_gather.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int, C.c_int,
                                     C.c_int, C.c_int]
         L.ogsref_scatter.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_int, C.c_int,
@@ -159,6 +162,11 @@ class RefOperator:
         ogsref().ogsref_gather_scatter(self._h, _ptr(v), v.size, TYPES[v.dtype.name], k, _code(OPS, op),
                                        _code(TRANS, trans))
         return v
+
+    def time_gather_scatter(self, v: np.ndarray, k: int, op="add", trans="sym", warm=2, reps=5) -> float:
+        """Mean seconds per GatherScatter of the reference's code on one held field."""
+        return ogsref().ogsref_time_gather_scatter(self._h, _ptr(v), v.size, TYPES[v.dtype.name], k,
+                                                   _code(OPS, op), _code(TRANS, trans), warm, reps)
 
     def gather(self, gv: np.ndarray, v: np.ndarray, k: int, op="add", trans="trans"):
         ogsref().ogsref_gather(self._h, _ptr(gv), gv.size, _ptr(v), v.size, TYPES[v.dtype.name], k,

@@ -9,6 +9,7 @@
 // order): the reference's setup (ogsSetup.cpp) runs the MPI exchanges and is
 // not compiled here.  occa.hpp and mpi.h in this directory stand in for the
 // two libraries the reference's headers name; no device path is called.
+#include <chrono>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -82,6 +83,20 @@ void gs_typed(RefOp* h, void* v, int64_t n, int k, int op, int trans) {
   from_memory(v, m, n);
 }
 
+// Mean seconds of `reps` GatherScatter calls on one field held across the
+// calls (as dawgs' PerformanceTest holds it), after `warm` untimed calls;
+// the field ends as after warm + reps calls.
+template <typename T>
+double time_gs_typed(RefOp* h, void* v, int64_t n, int k, int op, int trans, int warm, int reps) {
+  memory<T> m = to_memory<T>(v, n);
+  for (int i = 0; i < warm; ++i) h->op.GatherScatter(m, k, op_of(op), trans_of(trans));
+  const auto t0 = std::chrono::steady_clock::now();
+  for (int i = 0; i < reps; ++i) h->op.GatherScatter(m, k, op_of(op), trans_of(trans));
+  const auto t1 = std::chrono::steady_clock::now();
+  from_memory(v, m, n);
+  return std::chrono::duration<double>(t1 - t0).count() / (reps > 0 ? reps : 1);
+}
+
 template <typename T>
 void gather_typed(RefOp* h, void* gv, int64_t ngv, const void* v, int64_t nv, int k, int op, int trans) {
   memory<T> g = to_memory<T>(gv, ngv);
@@ -133,6 +148,17 @@ void ogsref_gather_scatter(void* h, void* v, int64_t n, int type, int k, int op,
     case 1: gs_typed<double>(r, v, n, k, op, trans); break;
     case 2: gs_typed<int>(r, v, n, k, op, trans); break;
     default: gs_typed<long long int>(r, v, n, k, op, trans); break;
+  }
+}
+
+double ogsref_time_gather_scatter(void* h, void* v, int64_t n, int type, int k, int op, int trans, int warm,
+                                  int reps) {
+  RefOp* r = static_cast<RefOp*>(h);
+  switch (type) {
+    case 0: return time_gs_typed<float>(r, v, n, k, op, trans, warm, reps);
+    case 1: return time_gs_typed<double>(r, v, n, k, op, trans, warm, reps);
+    case 2: return time_gs_typed<int>(r, v, n, k, op, trans, warm, reps);
+    default: return time_gs_typed<long long int>(r, v, n, k, op, trans, warm, reps);
   }
 }
 
