@@ -170,6 +170,9 @@ class Clocks:
         whole = self._stats(self.rows)
         out["timed_region_ms"] = 1e3 * (self._m1 - self._m0)
         out["sample_period_ms"] = 50
+        if out["timed_region_ms"] < 10 * out["sample_period_ms"]:
+            out["note"] = ("the timed region is shorter than ten sampling periods: its samples include the "
+                           "ones just after it; whole_run covers every kernel leg of the run")
         if whole is not None:
             # the kernel legs of this run (cold and warm loops, the reference
             # device algorithm, e2e): the region above is too short for many
