@@ -147,6 +147,31 @@ def test_interleaved_k_every_mode(cuda, oracle_mod, k):
         assert same_bits(from_dev(dv), ref.scatter(v0.copy(), want, k, trans)), ("scatter", trans)
 
 
+@pytest.mark.parametrize("k", [11584, 11585, 12001])
+def test_interleaved_k_at_the_divisor_limit(cuda, oracle_mod, k):
+    """The row lane of a thread is (32j + t) / k by a multiply-high for
+    k < 11585 and by a division above: both sides of that limit, single-mesh
+    and batched, on a small Signed mesh (every transpose)."""
+    base = mesh.box_ids(2, 2, 1, 2)
+    ids = signed_ids(base, seed=14)
+    g = ogs.ogs_t().Setup(ids.size, ids.copy(), None, ogs.Signed)
+    ref = oracle_mod.OracleOgs(ids.copy(), "signed")
+    for trans in TRANS:
+        v = values(k * ids.size, np.float64, "add", seed=k)
+        d = to_dev(v)
+        g.GatherScatter(d, k, ogs.Add, ogs.Transpose[{"sym": "Sym", "notrans": "NoTrans", "trans": "Trans"}[trans]])
+        want = ref.gather_scatter(v.copy(), k, "add", trans)
+        assert same_bits(from_dev(d), want), (trans, first_diff(from_dev(d), want))
+    gu = ogs.ogs_t().Setup(base.size, base.copy())
+    refu = oracle_mod.OracleOgs(base.copy(), "unsigned")
+    v = values(k * base.size, np.float64, "max", seed=k + 1)
+    d = to_dev(v)
+    b = ogs.ogs_batch_t([(gu, d, k, ogs.Max, ogs.Sym)])
+    b.GatherScatter()
+    torch.cuda.synchronize()
+    assert same_bits(from_dev(d), refu.gather_scatter(v.copy(), k, "max", "sym"))
+
+
 def test_c3_irregular_multifield(cuda, oracle_mod):
     """32x32x16 p=5 with a seeded element permutation; k=3 interleaved and k=8
     separate arrays; fp64/fp32 Add (U[-1,1]) and Mul (U[0.5,2])."""
