@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include "ogs_internal.hpp"
+#include "ogs_trace.hpp"
 
 struct ogs_batch_s {
   int type = 0;
@@ -318,6 +319,7 @@ ogs_status ogs_batch_set_fields(ogs_batch b, void* const* d_vs, void* stream) {
 
 ogs_status ogs_batch_gather_scatter(ogs_batch b, void* stream) {
   const char* fn = "ogs_batch_gather_scatter";
+  TraceRange trace(fn);
   if (!b) return set_error(OGS_EINVAL, "ogs_batch_gather_scatter: batch is NULL");
   int dev = -1;
   ogs_status s;
@@ -376,6 +378,7 @@ ogs_status ogs_batch_set_config(ogs_batch b, const ogs_batch_config* cfg, void* 
 
 ogs_status ogs_batch_tune_ex(ogs_batch b, void* stream, unsigned flags, ogs_batch_config* chosen) {
   const char* fn = "ogs_batch_tune";
+  TraceRange trace(fn);
   if (!b) return set_error(OGS_EINVAL, "ogs_batch_tune: batch is NULL");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const uint64_t key = batch_key(b);

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include "ogs_internal.hpp"
+#include "ogs_trace.hpp"
 
 #ifndef OGS_KERNEL
 #define OGS_KERNEL 0
@@ -234,6 +235,7 @@ int ogs_version(void) { return 10000; }
 
 ogs_status ogs_setup_ex(ogs_handle* out, int64_t N, int64_t* ids, int kind, int unique, unsigned flags) {
   if (!out) return set_error(OGS_EINVAL, "ogs_setup: out is NULL");
+  TraceRange trace("ogs_setup");
   *out = nullptr;
   const auto t0 = std::chrono::steady_clock::now();
   ogs_handle_s* h = new (std::nothrow) ogs_handle_s();
@@ -361,6 +363,7 @@ ogs_status ogs_scatter(ogs_handle h, void* d_v, const void* d_gv, int k, int typ
 
 ogs_status ogs_gather_scatter_host(ogs_handle h, void* v, int k, int type, int op, int trans, void* stream) {
   const char* fn = "ogs_gather_scatter_host";
+  TraceRange trace(fn);
   ogs_status s = check_common(h, k, type, trans, fn);
   if (s == OGS_OK) s = check_writes(h, fn);
   if (s == OGS_OK) s = check_op(op, fn);
@@ -514,6 +517,7 @@ ogs_status host_pipeline_gs_rows(ogs_handle_s* h, int mode, char* dv, char* dgv,
 ogs_status ogs_gather_host(ogs_handle h, void* gv, const void* v, int k, int type, int op, int trans,
                            void* stream) {
   const char* fn = "ogs_gather_host";
+  TraceRange trace(fn);
   ogs_status s = check_common(h, k, type, trans, fn);
   if (s == OGS_OK) s = check_op(op, fn);
   if (s != OGS_OK) return s;
@@ -549,6 +553,7 @@ ogs_status ogs_gather_host(ogs_handle h, void* gv, const void* v, int k, int typ
 
 ogs_status ogs_scatter_host(ogs_handle h, void* v, const void* gv, int k, int type, int trans, void* stream) {
   const char* fn = "ogs_scatter_host";
+  TraceRange trace(fn);
   ogs_status s = check_common(h, k, type, trans, fn);
   if (s == OGS_OK) s = check_writes(h, fn);
   if (s != OGS_OK) return s;

@@ -36,6 +36,7 @@
 #include <cuda_runtime.h>
 
 #include "ogs_internal.hpp"
+#include "ogs_trace.hpp"
 
 namespace ogsgb {
 namespace {
@@ -381,6 +382,7 @@ cudaError_t inclusive_sum(Scratch& sc, const T* in, T* out, int64_t n, cudaStrea
 
 ogs_status build_device_layout(ogs_handle_s* h, const int32_t* rsT, const int32_t* ciT, const int32_t* rsN,
                                const int32_t* ciN, void* stream) {
+  TraceRange trace("ogs_setup: layout on the GPU");
   const cudaStream_t st = static_cast<cudaStream_t>(stream);
   HostLayout& L = h->lay;
   L = HostLayout{};
@@ -642,6 +644,7 @@ ogs_status build_device_layout(ogs_handle_s* h, const int32_t* rsT, const int32_
 }
 
 ogs_status build_device_maps(ogs_handle_s* h, int64_t N, int64_t* ids, int kind, int unique, bool layout) {
+  TraceRange trace("ogs_setup: maps on the GPU");
   if (kind == OGS_HALO)
     return set_error(OGS_EINVAL, "ogs_setup: Halo handles are not part of the single-rank path");
   if (kind != OGS_UNSIGNED && kind != OGS_SIGNED) return set_error(OGS_EINVAL, "ogs_setup: unknown kind");

@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include "ogs_internal.hpp"
+#include "ogs_trace.hpp"
 
 using namespace ogsgb;
 
@@ -130,6 +131,7 @@ ogs_status finish_locked(ogs_halo h, void* v, int k, int type, int trans, const 
 
 ogs_status device_call(ogs_halo h, void* d_v, int k, int type, int trans, const ogs_exchange* x, void* stream,
                        int which, const char* fn) {
+  TraceRange trace(fn);
   ogs_status s = check_args(h, k, type, fn);
   if (s != OGS_OK) return s;
   if (!d_v && h->N > 0 && (h->NhaloT > 0)) return set_error(OGS_EINVAL, std::string(fn) + ": field is NULL");
@@ -142,6 +144,7 @@ ogs_status device_call(ogs_halo h, void* d_v, int k, int type, int trans, const 
 // Host field: staged through the device, the whole step, copied back.
 ogs_status host_call(ogs_halo h, void* v, int k, int type, int trans, const ogs_exchange* x, void* stream,
                      const char* fn) {
+  TraceRange trace(fn);
   ogs_status s = check_args(h, k, type, fn);
   if (s != OGS_OK) return s;
   if (h->NhaloT == 0) {  // nothing of v is read or written; the exchange still runs

@@ -47,6 +47,7 @@
 #include <cuda_runtime.h>
 
 #include "ogs_internal.hpp"
+#include "ogs_trace.hpp"
 
 namespace ogsgb {
 namespace {
@@ -266,6 +267,7 @@ std::vector<TableSlot*> free_slots(ogs_server_s* s, int want) {
 // Launch one group of a lane's requests of one value type on the lane's
 // compute stream, after the lane's copies in; queue their copies out.
 int launch_group(ogs_server_s* s, Lane& lane, TableSlot& slot, const std::vector<Req*>& grp, int type) {
+  TraceRange trace(&lane == &s->lanes[0] ? "ogs_server: small-field batch" : "ogs_server: large-field batch");
   const int n = static_cast<int>(grp.size());
   slot.h_starts[0] = 0;
   int plain = 1;

@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 
 #include "ogs_internal.hpp"
+#include "ogs_trace.hpp"
 
 namespace ogsgb {
 namespace {
@@ -75,6 +76,7 @@ size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 }  // namespace
 
 ogs_status build_host_maps(ogs_handle_s* h, int64_t N, int64_t* ids, int kind, int unique) {
+  TraceRange trace("ogs_setup: maps on the host");
   if (kind == OGS_HALO)
     return set_error(OGS_EINVAL, "ogs_setup: Halo handles are not part of the single-rank path");
   if (kind != OGS_UNSIGNED && kind != OGS_SIGNED)
@@ -180,6 +182,7 @@ ogs_status build_host_maps(ogs_handle_s* h, int64_t N, int64_t* ids, int kind, i
 }
 
 void build_layout(ogs_handle_s* h) {
+  TraceRange trace("ogs_setup: layout on the host");
   HostLayout& L = h->lay;
   const bool sgn = (h->kind == OGS_SIGNED);
   const int64_t R = h->NlocalT;
