@@ -647,9 +647,13 @@ def run_ours(a):
     # setup wall time, maps built on the GPU (the default at this size) and on the host
     setup_s = {"local_dofs": int(ids.size)}
     for how in ("device", "host"):
+        idc = ids.copy()  # Setup may rewrite its ids (unique)
+        torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        ogs.ogs_t().Setup(ids.size, ids.copy(), None, kind, ogs.Auto, unique, maps=how).Free()
+        h = ogs.ogs_t().Setup(ids.size, idc, None, kind, ogs.Auto, unique, maps=how)
+        torch.cuda.synchronize(dev)
         setup_s[f"{how}_maps_s"] = time.perf_counter() - t0
+        h.Free()
     tcode, ocode = TYPE_CODE[a.dtype], OP_CODE[a.op]
     s = np.dtype(a.dtype).itemsize
     pristine = torch.from_numpy(v).to(dev)
