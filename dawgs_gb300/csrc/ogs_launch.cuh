@@ -1,10 +1,19 @@
 // ogs_launch.cuh -- per-type launch dispatch shared by ogs_kern_*.cu.
 //
 // Exact-degree rows run on the warp pipeline with cp.async-staged gathers
-// (ogs_async.cuh; -DOGS_ASYNC=0: the register pipeline of ogs_warp.cuh) for
-// every k and layout; rows above degree 8 on the direct CTA kernel
-// (ogs_kernels.cuh).  Building with -DOGS_KERNEL=2 runs the direct CTA
+// (ogs_async.cuh) for GatherScatter and for every k > 1 and layout; Gather
+// and Scatter of one component run on the register pipeline of ogs_warp.cuh
+// (-DOGS_GATHER_REGISTERS=0: on the cp.async one too; -DOGS_ASYNC=0: the
+// register pipeline everywhere).  Rows above degree 8 run on the direct CTA
+// kernel (ogs_kernels.cuh).  Building with -DOGS_KERNEL=2 runs the direct CTA
 // kernel for every row instead (for comparisons).
+//
+// Why the split: a GatherScatter row is read and written in place, and two
+// tiles' gathers in flight through the shared-memory ring beat one in
+// registers (24^3 p=7 fp64: 28.3 vs 31.6 us); a Gather writes one value per
+// row and a Scatter reads one per row, and there the ring's shared-memory
+// fills cost more than they hide (Gather Trans 25.2 vs 26.6 us, Scatter
+// NoTrans 29.9 vs 30.6 us).
 #pragma once
 
 #include "ogs_async.cuh"
@@ -12,14 +21,23 @@
 #ifndef OGS_KERNEL
 #define OGS_KERNEL 0
 #endif
+#ifndef OGS_GATHER_REGISTERS
+#define OGS_GATHER_REGISTERS 1
+#endif
 
 namespace ogsgb {
 
 template <typename T, int OP, int MODE>
 inline cudaError_t launch_mode(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
-  if constexpr (OGS_KERNEL == 2) return launch_direct<T, OP, MODE>(m, f, pat, s);
-  else if constexpr (OGS_ASYNC != 0) return launch_async<T, OP, MODE>(m, f, pat, s);
-  else return launch_warp<T, OP, MODE>(m, f, pat, s);
+  if constexpr (OGS_KERNEL == 2) {
+    return launch_direct<T, OP, MODE>(m, f, pat, s);
+  } else if constexpr (OGS_ASYNC != 0) {
+    if constexpr (MODE != kModeGS && OGS_GATHER_REGISTERS != 0)
+      if (f.K == 1 && !f.is_many) return launch_warp_k1<T, OP, MODE>(m, f, pat, s);
+    return launch_async<T, OP, MODE>(m, f, pat, s);
+  } else {
+    return launch_warp<T, OP, MODE>(m, f, pat, s);
+  }
 }
 
 template <typename T, int MODE>

@@ -170,9 +170,10 @@ enum KLayout : int {
                     // the grid sweeps that array
 };
 
-template <typename T, int OP, int MODE, int KL>
+template <typename T, int OP, int MODE, int KL, bool PLAIN>
 __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const DevMaps m, const FieldArgs f,
-                                                                         const Pattern pat) {
+                                                                         const Pattern pat_in) {
+  const Pattern pat = PLAIN ? Pattern{0, 0, 0, 0} : pat_in;
   const int lane = static_cast<int>(threadIdx.x) & 31;
   const int64_t W = static_cast<int64_t>(gridDim.x) * (kBlock / 32);
   const int K = KL == kK1 ? 1 : f.K;
@@ -180,10 +181,10 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const D
   const int64_t nitems = nw * K;
   int64_t i = static_cast<int64_t>(blockIdx.x) * (kBlock / 32) + (threadIdx.x >> 5);
   if (i >= nitems) return;
-  const bool use_mask = (pat.gather_n || pat.scatter_n) && m.signed_maps;
-  const bool gmask = pat.gather_n != 0;
-  const int smode = pat.scatter_n;
-  const bool gslib = pat.gslib != 0;
+  const bool use_mask = !PLAIN && (pat.gather_n || pat.scatter_n) && m.signed_maps;
+  const bool gmask = !PLAIN && pat.gather_n != 0;
+  const int smode = PLAIN ? 0 : pat.scatter_n;
+  const bool gslib = !PLAIN && pat.gslib != 0;
   const int64_t stride = KL == kKInterleaved ? K : 1;
   auto tile_of = [&](int64_t item) {
     return static_cast<int>(KL == kKMany ? item % nw : (KL == kKInterleaved ? item / K : item));
@@ -231,14 +232,14 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const D
 }
 
 // CTAs of the warp kernel resident per SM, once per instantiation and device.
-template <typename T, int OP, int MODE, int KL>
+template <typename T, int OP, int MODE, int KL, bool PLAIN>
 inline int warp_grid(int64_t nitems) {
   static DeviceCache cache;
   int dev = 0;
   cudaGetDevice(&dev);
   const int cached = cache.get(dev, [dev] {
     int bps = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_warp_kernel<T, OP, MODE, KL>, kBlock, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ogs_warp_kernel<T, OP, MODE, KL, PLAIN>, kBlock, 0);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     return (bps > 0 ? bps : 1) * (sms > 0 ? sms : 1);
   });
@@ -246,19 +247,45 @@ inline int warp_grid(int64_t nitems) {
   return static_cast<int>(need < cached ? need : cached);
 }
 
+template <typename T, int OP, int MODE, int KL, bool PLAIN>
+inline void launch_warp_kl(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
+  const int64_t nitems = static_cast<int64_t>(m.nwtiles) * (KL == kK1 ? 1 : f.K);
+  const int grid = warp_grid<T, OP, MODE, KL, PLAIN>(nitems);
+  ogs_warp_kernel<T, OP, MODE, KL, PLAIN><<<grid, kBlock, 0, s>>>(m, f, pat);
+}
+
+template <typename T, int OP, int MODE, bool PLAIN>
+inline void launch_warp_plain(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
+  if (f.is_many) launch_warp_kl<T, OP, MODE, kKMany, PLAIN>(m, f, pat, s);
+  else if (f.K == 1) launch_warp_kl<T, OP, MODE, kK1, PLAIN>(m, f, pat, s);
+  else launch_warp_kl<T, OP, MODE, kKInterleaved, PLAIN>(m, f, pat, s);
+}
+
+// One component in one array: the k = 1 register pipeline only.
+template <typename T, int OP, int MODE>
+inline cudaError_t launch_warp_k1(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
+  if (m.nwtiles > 0) {
+    const bool plain = !pat.gather_n && !pat.scatter_n && !pat.limit_n && !pat.gslib;
+    if (plain) launch_warp_kl<T, OP, MODE, kK1, true>(m, f, pat, s);
+    else launch_warp_kl<T, OP, MODE, kK1, false>(m, f, pat, s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  if (m.ngtiles > 0) {
+    DevMaps g = m;
+    g.tiles = m.gtiles;
+    g.ntiles = m.ngtiles;
+    return launch_direct<T, OP, MODE>(g, f, pat, s);
+  }
+  return cudaSuccess;
+}
+
 template <typename T, int OP, int MODE>
 inline cudaError_t launch_warp(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
   if (m.nwtiles > 0) {
-    if (f.is_many) {
-      const int grid = warp_grid<T, OP, MODE, kKMany>(static_cast<int64_t>(m.nwtiles) * f.K);
-      ogs_warp_kernel<T, OP, MODE, kKMany><<<grid, kBlock, 0, s>>>(m, f, pat);
-    } else if (f.K == 1) {
-      const int grid = warp_grid<T, OP, MODE, kK1>(static_cast<int64_t>(m.nwtiles));
-      ogs_warp_kernel<T, OP, MODE, kK1><<<grid, kBlock, 0, s>>>(m, f, pat);
-    } else {
-      const int grid = warp_grid<T, OP, MODE, kKInterleaved>(static_cast<int64_t>(m.nwtiles) * f.K);
-      ogs_warp_kernel<T, OP, MODE, kKInterleaved><<<grid, kBlock, 0, s>>>(m, f, pat);
-    }
+    const bool plain = !pat.gather_n && !pat.scatter_n && !pat.limit_n && !pat.gslib;
+    if (plain) launch_warp_plain<T, OP, MODE, true>(m, f, pat, s);
+    else launch_warp_plain<T, OP, MODE, false>(m, f, pat, s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
