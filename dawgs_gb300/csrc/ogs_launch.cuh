@@ -1,19 +1,20 @@
 // ogs_launch.cuh -- per-type launch dispatch shared by ogs_kern_*.cu.
 //
-// Exact-degree rows run on the warp pipeline with cp.async-staged gathers
-// (ogs_async.cuh) for GatherScatter and for every k > 1 and layout; Gather
-// and Scatter of one component run on the register pipeline of ogs_warp.cuh
-// (-DOGS_GATHER_REGISTERS=0: on the cp.async one too; -DOGS_ASYNC=0: the
-// register pipeline everywhere).  Rows above degree 8 run on the direct CTA
-// kernel (ogs_kernels.cuh).  Building with -DOGS_KERNEL=2 runs the direct CTA
-// kernel for every row instead (for comparisons).
+// Exact-degree rows of GatherScatter run on the warp pipeline with
+// cp.async-staged gathers (ogs_async.cuh), those of Gather and Scatter on the
+// register pipeline of ogs_warp.cuh (-DOGS_GATHER_REGISTERS=0: everything on
+// the cp.async one; -DOGS_ASYNC=0: everything on the register one).  Rows
+// above degree 8 run on the direct CTA kernel (ogs_kernels.cuh).  Building
+// with -DOGS_KERNEL=2 runs the direct CTA kernel for every row instead (for
+// comparisons).
 //
 // Why the split: a GatherScatter row is read and written in place, and two
 // tiles' gathers in flight through the shared-memory ring beat one in
-// registers (24^3 p=7 fp64: 28.3 vs 31.6 us); a Gather writes one value per
-// row and a Scatter reads one per row, and there the ring's shared-memory
-// fills cost more than they hide (Gather Trans 25.2 vs 26.6 us, Scatter
-// NoTrans 29.9 vs 30.6 us).
+// registers (24^3 p=7 fp64: 28.3 vs 31.6 us; 32x32x16 p=5 permuted k=3: 41.1
+// vs 42.4 us); a Gather writes one value per row and a Scatter reads one per
+// row, and there the ring's shared-memory fills cost more than they hide
+// (24^3 p=7: Gather Trans 25.2 vs 26.6 us, Scatter NoTrans 29.9 vs 30.6 us;
+// k=3: Gather 32.9 vs 52.0 us, Scatter 47.3 vs 50.9 us).
 #pragma once
 
 #include "ogs_async.cuh"
@@ -32,9 +33,8 @@ inline cudaError_t launch_mode(const DevMaps& m, const FieldArgs& f, Pattern pat
   if constexpr (OGS_KERNEL == 2) {
     return launch_direct<T, OP, MODE>(m, f, pat, s);
   } else if constexpr (OGS_ASYNC != 0) {
-    if constexpr (MODE != kModeGS && OGS_GATHER_REGISTERS != 0)
-      if (f.K == 1 && !f.is_many) return launch_warp_k1<T, OP, MODE>(m, f, pat, s);
-    return launch_async<T, OP, MODE>(m, f, pat, s);
+    if constexpr (MODE != kModeGS && OGS_GATHER_REGISTERS != 0) return launch_warp<T, OP, MODE>(m, f, pat, s);
+    else return launch_async<T, OP, MODE>(m, f, pat, s);
   } else {
     return launch_warp<T, OP, MODE>(m, f, pat, s);
   }

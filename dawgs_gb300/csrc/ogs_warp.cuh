@@ -189,11 +189,26 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const D
   auto tile_of = [&](int64_t item) {
     return static_cast<int>(KL == kKMany ? item % nw : (KL == kKInterleaved ? item / K : item));
   };
+  // k > 1 interleaved: item (tile, part j); thread t works row lane
+  // (32j + t) / k, component (32j + t) % k, as in the cp.async pipeline
+  const uint32_t kmagic = KL == kKInterleaved && K > 1 ? 0xFFFFFFFFu / static_cast<uint32_t>(K) + 1u : 0u;
+  auto row_lane = [&](int64_t item, int& comp) {
+    if (KL != kKInterleaved) {
+      comp = KL == kKMany ? static_cast<int>(item / nw) : 0;
+      return lane;
+    }
+    const uint32_t u = static_cast<uint32_t>(item % K) * 32u + static_cast<uint32_t>(lane);
+    const int rl = static_cast<int>(K < 11585 ? __umulhi(u, kmagic) : u / static_cast<uint32_t>(K));
+    comp = static_cast<int>(u) - rl * K;
+    return rl;
+  };
 
   int tcur = tile_of(i);
   Tile cur = m.wtiles[tcur];
   WarpState scur;
-#define OGS_LOAD_CUR(D) warp_load_state<MODE, D>(m.b[D], cur, m.wemask, tcur, use_mask, pat, lane, scur)
+  int ccur;
+  int rcur = row_lane(i, ccur);
+#define OGS_LOAD_CUR(D) warp_load_state<MODE, D>(m.b[D], cur, m.wemask, tcur, use_mask, pat, rcur, scur)
   OGS_DEGREE_SWITCH(cur.bucket, OGS_LOAD_CUR)
 #undef OGS_LOAD_CUR
   Tile nxt{};
@@ -201,25 +216,26 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const D
 
   T* gv = static_cast<T*>(f.gv);
   for (;;) {
-    const int k0 = KL == kKMany ? static_cast<int>(i / nw) : (KL == kKInterleaved ? static_cast<int>(i % K) : 0);
+    const int k0 = ccur;
     const T* src = (MODE == kModeScatter) ? nullptr : field_base<T>(f, k0);
     T* dst = (MODE == kModeGather) ? nullptr : field_base<T>(f, k0);
     T V[kWarpSlots];
-#define OGS_VALS(D) warp_load_vals<T, MODE, D>(scur, src, gv, stride, K, k0, gmask, lane, V)
+#define OGS_VALS(D) warp_load_vals<T, MODE, D>(scur, src, gv, stride, K, k0, gmask, rcur, V)
     OGS_DEGREE_SWITCH(cur.bucket, OGS_VALS)
 #undef OGS_VALS
     const bool more = i + W < nitems;
     WarpState snxt;
     Tile nn{};
-    int tnxt = 0;
+    int tnxt = 0, cnxt = 0, rnxt = lane;
     if (more) {
       tnxt = tile_of(i + W);
-#define OGS_LOAD_NXT(D) warp_load_state<MODE, D>(m.b[D], nxt, m.wemask, tnxt, use_mask, pat, lane, snxt)
+      rnxt = row_lane(i + W, cnxt);
+#define OGS_LOAD_NXT(D) warp_load_state<MODE, D>(m.b[D], nxt, m.wemask, tnxt, use_mask, pat, rnxt, snxt)
       OGS_DEGREE_SWITCH(nxt.bucket, OGS_LOAD_NXT)
 #undef OGS_LOAD_NXT
       if (i + 2 * W < nitems) nn = m.wtiles[tile_of(i + 2 * W)];
     }
-#define OGS_FOLD(D) warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, k0, gmask, smode, gslib, lane, V)
+#define OGS_FOLD(D) warp_fold_store<T, OP, MODE, D>(scur, dst, gv, stride, K, k0, gmask, smode, gslib, rcur, V)
     OGS_DEGREE_SWITCH(cur.bucket, OGS_FOLD)
 #undef OGS_FOLD
     if (!more) break;
@@ -228,8 +244,11 @@ __global__ void __launch_bounds__(kBlock, OGS_WARP_MINB) ogs_warp_kernel(const D
     scur = snxt;
     nxt = nn;
     tcur = tnxt;
+    ccur = cnxt;
+    rcur = rnxt;
   }
 }
+
 
 // CTAs of the warp kernel resident per SM, once per instantiation and device.
 template <typename T, int OP, int MODE, int KL, bool PLAIN>
@@ -259,25 +278,6 @@ inline void launch_warp_plain(const DevMaps& m, const FieldArgs& f, Pattern pat,
   if (f.is_many) launch_warp_kl<T, OP, MODE, kKMany, PLAIN>(m, f, pat, s);
   else if (f.K == 1) launch_warp_kl<T, OP, MODE, kK1, PLAIN>(m, f, pat, s);
   else launch_warp_kl<T, OP, MODE, kKInterleaved, PLAIN>(m, f, pat, s);
-}
-
-// One component in one array: the k = 1 register pipeline only.
-template <typename T, int OP, int MODE>
-inline cudaError_t launch_warp_k1(const DevMaps& m, const FieldArgs& f, Pattern pat, cudaStream_t s) {
-  if (m.nwtiles > 0) {
-    const bool plain = !pat.gather_n && !pat.scatter_n && !pat.limit_n && !pat.gslib;
-    if (plain) launch_warp_kl<T, OP, MODE, kK1, true>(m, f, pat, s);
-    else launch_warp_kl<T, OP, MODE, kK1, false>(m, f, pat, s);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-  }
-  if (m.ngtiles > 0) {
-    DevMaps g = m;
-    g.tiles = m.gtiles;
-    g.ntiles = m.ngtiles;
-    return launch_direct<T, OP, MODE>(g, f, pat, s);
-  }
-  return cudaSuccess;
 }
 
 template <typename T, int OP, int MODE>
