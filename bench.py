@@ -1062,6 +1062,22 @@ def run_sweep(a):
                   for j in range(8)]
             gs(f"32x32x16 p=5 perm {str(dt)[6:]} {nm} k=8 arrays", g, None, 8, op, 16 * s * ids.size + idx_bytes(g),
                many=vs)
+    # Gather (Trans) and Scatter (NoTrans) of k = 3 interleaved components on
+    # the Signed unique handle of the same mesh
+    sa = ids.copy()
+    sg = ogs.ogs_t().Setup(sa.size, sa, None, ogs.Signed, ogs.Auto, True)
+    for dt, s in ((torch.float64, 8), (torch.float32, 4)):
+        tc = tcode[dt]
+        gv3 = torch.zeros(3 * sg.Ngather, dtype=dt, device=dev)
+        x3 = torch.from_numpy(mesh.uniform_values(3 * ids.size, np.float64, -1.0, 1.0, 9)).to(dev).to(dt)
+        ab3 = 3 * s * (ids.size + sg.Ngather) + idx_bytes(sg)
+        for nm, fn in (("Gather Trans", lambda: L.ogs_gather(sg.handle, gv3.data_ptr(), x3.data_ptr(), 3, tc, 0, 2,
+                                                             st.cuda_stream)),
+                       ("Scatter NoTrans", lambda: L.ogs_scatter(sg.handle, x3.data_ptr(), gv3.data_ptr(), 3, tc, 1,
+                                                                 st.cuda_stream))):
+            case = f"32x32x16 p=5 perm {str(dt)[6:]} {nm} k=3"
+            if wanted(case):
+                emit(case, sg, 3, timeit(fn), ab3, timeit(fn, cold=False))
     return 0
 
 
