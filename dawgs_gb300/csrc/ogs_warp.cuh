@@ -1,12 +1,16 @@
-// ogs_warp.cuh -- persistent, warp-pipelined gather-scatter kernel.
+// ogs_warp.cuh -- persistent, warp-pipelined gather-scatter kernel with the
+// gathered values in registers: the kernel of Gather and Scatter (a row
+// writes or reads one gathered value, and holding a second tile's gathers in
+// the shared-memory ring of ogs_async.cuh costs more there than it hides),
+// and the fold and state helpers the cp.async pipeline shares.
 //
 // Arithmetic as in ogs_kernels.cuh (one fold per row from the op identity
 // over the members in ascending local index: ogsOperator.cpp:60-97, 206-238,
 // 311-360).  The data movement is organised per warp, with no block-level
 // synchronisation at all:
 //
-//  * Work items are warp tiles (and, for separate arrays, the array; see
-//    KLayout).  A warp tile holds 32 lanes x
+//  * Work items are warp tiles (for k > 1 interleaved, a tile's parts; for
+//    separate arrays, the array; see KLayout).  A warp tile holds 32 lanes x
 //    kWarpEntries member entries of one exact-degree bucket: lane l owns rows
 //    l, l+32, ... of the tile, each with its d members.  Tiles are ordered by
 //    first row; warp w of the grid takes items w, w+W, w+2W, ... so the grid
@@ -160,9 +164,10 @@ __device__ __forceinline__ void warp_fold_store(const WarpState& s, T* dst, T* g
 // How the k components of a field map onto work items.
 enum KLayout : int {
   kK1 = 0,          // k = 1: item = tile
-  kKInterleaved = 1,  // v[c + n*k], k > 1: item = (tile, component), tile-major,
-                      // so the k warps of one tile run side by side and share
-                      // the sectors of each node's k values.  (One item per
+  kKInterleaved = 1,  // v[c + n*k], k > 1: item = (tile, part), tile-major;
+                      // part j takes the tile's (row lane, component) units
+                      // 32j .. 32j+31, so neighbouring threads read the k
+                      // values of one node in one instruction.  (One item per
                       // tile looping over the components was slower: 86 vs
                       // 66 us for k = 3 on 3.5 M permuted nodes.)
   kKMany = 2,       // k separate arrays: item = (array, tile), array-major, so
