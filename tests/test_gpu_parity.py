@@ -150,8 +150,9 @@ def test_interleaved_k_every_mode(cuda, oracle_mod, k):
 @pytest.mark.parametrize("k", [11584, 11585, 12001])
 def test_interleaved_k_at_the_divisor_limit(cuda, oracle_mod, k):
     """The row lane of a thread is (32j + t) / k by a multiply-high for
-    k < 11585 and by a division above: both sides of that limit, single-mesh
-    and batched, on a small Signed mesh (every transpose)."""
+    k < 11585 and by a division above: both sides of that limit, for
+    GatherScatter (every transpose, Signed), Gather and Scatter (Signed
+    unique) and the batched kernel, on a small mesh."""
     base = mesh.box_ids(2, 2, 1, 2)
     ids = signed_ids(base, seed=14)
     g = ogs.ogs_t().Setup(ids.size, ids.copy(), None, ogs.Signed)
@@ -162,6 +163,21 @@ def test_interleaved_k_at_the_divisor_limit(cuda, oracle_mod, k):
         g.GatherScatter(d, k, ogs.Add, ogs.Transpose[{"sym": "Sym", "notrans": "NoTrans", "trans": "Trans"}[trans]])
         want = ref.gather_scatter(v.copy(), k, "add", trans)
         assert same_bits(from_dev(d), want), (trans, first_diff(from_dev(d), want))
+    # Gather and Scatter (the register pipeline) on a Signed unique handle
+    ids_a, ids_b = base.copy(), base.copy()
+    gq = ogs.ogs_t().Setup(ids_a.size, ids_a, None, ogs.Signed, ogs.Auto, True)
+    refq = oracle_mod.OracleOgs(ids_b, "signed", unique=True)
+    v = values(k * base.size, np.float64, "add", seed=k + 2)
+    for trans, T in (("trans", ogs.Trans), ("notrans", ogs.NoTrans)):
+        want = np.zeros(k * gq.Ngather, np.float64)
+        refq.gather(want, v, k, "add", trans)
+        dgv = torch.zeros(k * gq.Ngather, dtype=torch.float64, device="cuda")
+        gq.Gather(dgv, to_dev(v), k, ogs.Add, T)
+        assert same_bits(from_dev(dgv), want), ("gather", trans)
+        v0 = values(k * base.size, np.float64, "add", seed=k + 3)
+        dv = to_dev(v0)
+        gq.Scatter(dv, to_dev(want), k, T)
+        assert same_bits(from_dev(dv), refq.scatter(v0.copy(), want, k, trans)), ("scatter", trans)
     gu = ogs.ogs_t().Setup(base.size, base.copy())
     refu = oracle_mod.OracleOgs(base.copy(), "unsigned")
     v = values(k * base.size, np.float64, "max", seed=k + 1)
