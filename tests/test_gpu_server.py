@@ -7,7 +7,7 @@ import pytest
 import torch
 
 from dawgs_gb300 import mesh, ogs
-from helpers import first_diff, same_bits, signed_ids, values
+from helpers import first_diff, random_ids, same_bits, signed_ids, values
 
 pytestmark = pytest.mark.gpu
 
@@ -16,10 +16,13 @@ TRN = {ogs.Sym: "sym", ogs.NoTrans: "notrans", ogs.Trans: "trans"}
 DT = [np.float64, np.float32, np.int64, np.int32]
 
 
-def make_meshes(oracle_mod, n, seed):
+def make_meshes(oracle_mod, n, seed, general=False):
     out = []
     for j, (nx, ny, nz, p) in enumerate(mesh.mesh_mix(n, seed, lo=1, hi=7, pmax=5)):
         ids = mesh.box_ids(nx, ny, nz, p)
+        if general and j % 2 == 0:
+            # rows of up to ~40 members: the general-tile launch beside the batch
+            ids = np.concatenate([ids, random_ids(2000, 60, seed=j) + 10 ** 7])
         kind = ogs.Unsigned
         if j % 3 == 2:
             ids = signed_ids(ids, seed=j)
@@ -57,9 +60,10 @@ def run(server, meshes, reqs):
     return host
 
 
-@pytest.mark.parametrize("budget_mb", [4096, 1])
-def test_served_results_equal_alone_and_oracle(cuda, oracle_mod, budget_mb):
-    meshes = make_meshes(oracle_mod, 6, seed=3)
+@pytest.mark.parametrize("budget_mb,general", [(4096, False), (1, False), (4096, True)],
+                         ids=["4096MB", "1MB", "4096MB-general-rows"])
+def test_served_results_equal_alone_and_oracle(cuda, oracle_mod, budget_mb, general):
+    meshes = make_meshes(oracle_mod, 6, seed=3, general=general)
     server = ogs.ogs_server_t(field_budget_bytes=budget_mb << 20, max_inflight=64, max_batch=32)
     mids = [server.add_mesh(g) for g, _, _ in meshes]
     assert mids == list(range(len(meshes)))
