@@ -117,7 +117,8 @@ def test_interleaved_k_every_mode(cuda, oracle_mod, k):
     """Interleaved k > 1: a tile's 32 row lanes x k components are split over
     its k warp items, so a thread's row lane and component depend on k (powers
     of two and not, k > 32).  GatherScatter on Unsigned and Signed handles
-    (every transpose), Gather and Scatter on a Signed unique handle."""
+    (every transpose), Gather and Scatter of every type on a Signed unique
+    handle."""
     base = mesh.permute_elements(mesh.box_ids(6, 5, 4, 3), 3, seed=11)
     for kind in ("unsigned", "signed"):
         ids = base if kind == "unsigned" else signed_ids(base, seed=12)
@@ -134,17 +135,18 @@ def test_interleaved_k_every_mode(cuda, oracle_mod, k):
     ids_a, ids_b = base.copy(), base.copy()
     g = ogs.ogs_t().Setup(ids_a.size, ids_a, None, ogs.Signed, ogs.Auto, True)
     ref = oracle_mod.OracleOgs(ids_b, "signed", unique=True)
-    v = values(k * base.size, np.float64, "add", seed=60 + k)
-    for trans, T in (("trans", ogs.Trans), ("notrans", ogs.NoTrans)):
-        want = np.zeros(k * g.Ngather, np.float64)
-        ref.gather(want, v, k, "add", trans)
-        dgv = torch.zeros(k * g.Ngather, dtype=torch.float64, device="cuda")
-        g.Gather(dgv, to_dev(v), k, ogs.Add, T)
-        assert same_bits(from_dev(dgv), want), ("gather", trans)
-        v0 = values(k * base.size, np.float64, "add", seed=61 + k)
-        dv = to_dev(v0)
-        g.Scatter(dv, to_dev(want), k, T)
-        assert same_bits(from_dev(dv), ref.scatter(v0.copy(), want, k, trans)), ("scatter", trans)
+    for dtype, op in ((np.float64, "add"), (np.int32, "max"), (np.float32, "mul"), (np.int64, "min")):
+        v = values(k * base.size, dtype, op, seed=60 + k)
+        for trans, T in (("trans", ogs.Trans), ("notrans", ogs.NoTrans)):
+            want = np.zeros(k * g.Ngather, dtype)
+            ref.gather(want, v, k, op, trans)
+            dgv = torch.zeros(k * g.Ngather, dtype=_TORCH[dtype], device="cuda")
+            g.Gather(dgv, to_dev(v), k, ogs.Op[op.capitalize()], T)
+            assert same_bits(from_dev(dgv), want), ("gather", dtype, op, trans)
+            v0 = values(k * base.size, dtype, "add", seed=61 + k)
+            dv = to_dev(v0)
+            g.Scatter(dv, to_dev(want), k, T)
+            assert same_bits(from_dev(dv), ref.scatter(v0.copy(), want, k, trans)), ("scatter", dtype, trans)
 
 
 @pytest.mark.parametrize("k", [11584, 11585, 12001])
